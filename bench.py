@@ -1,0 +1,376 @@
+"""Benchmark: one BCGSI+P-1S QR of a tall-skinny FP64 matrix on one GB300.
+
+A "step" is one full QR (the reference's bcgsi2P1s, SRC/orth.c:48-222) of the
+m x n matrix X = U diag(sigma) W^T (U, W Q factors of seeded Gaussians, sigma
+log-spaced from 1 to 1/kappa), m = 2^23, n = 512, s = 16, kappa = 1e6: the
+configuration the reference's headline metric is quoted on. Synthetic data of
+that construction stands in for any dataset (there is none).
+
+Per step the input is restored from a resident copy (a device-to-device copy
+outside the timed interval: the QR overwrites X in place); the QR itself is
+timed with CUDA events on the launching stream. X is 34 GB, far larger than the
+129 MB L2, so no L2 flush is needed between steps.
+
+Output: one JSON line (rank 0). `value` is ms per QR with X resident in HBM;
+`e2e` is the same QR through the orth.h host entry point with host buffers
+(host->device and device->host copies inside the timed interval); `roofline`
+is the dominant kernel's algorithmic rate against the measured peak of the pipe
+that bounds it; `cpu_baseline` times the oracle (the numpy/OpenBLAS restatement
+of the reference) on a bounded sample of the same workload on the host cores.
+
+`--impl reference` times the reference's CPU algorithm (the oracle restatement;
+the reference's own build cannot run on this host) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "one-synchronization-bcgs_gb300"))
+
+METRIC = "ms per BCGSI+P-1S QR (m=2^23, n=512, s=16, FP64 in/out)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--variant", default="bcgsi2P1s")
+    ap.add_argument("--m", type=int, default=1 << 23)
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--s", type=int, default=16)
+    ap.add_argument("--kappa", type=float, default=1e6)
+    ap.add_argument("--precision", choices=["auto", "fp64", "split"], default="auto")
+    ap.add_argument("--fp64-steps", type=int, default=1,
+                    help="timed FP64 QRs reported beside a split-precision run")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--cpu-rows", type=int, default=1 << 19,
+                    help="rows of the bounded CPU sample (time scaled to m)")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def alg_bytes_p1s(m: int, n: int, s: int) -> float:
+    """Algorithmic HBM bytes of one BCGSI+P-1S QR: one read of Q_{1:k-1} per
+    block step plus reading X, writing Q and writing+reading U once:
+    8 m [s P (P-1)/2 + 4 n] with P = n/s blocks."""
+    P = n // s
+    return 8.0 * m * (s * P * (P - 1) / 2.0 + 4.0 * n)
+
+
+def alg_flops_p1s(m: int, n: int, s: int) -> float:
+    """Algorithmic flops of one BCGSI+P-1S QR: 4 m n^2 + 8 m n s."""
+    return 4.0 * m * n * n + 8.0 * m * n * s
+
+
+def cpu_sample(args, rows: int):
+    """Time the oracle (numpy/OpenBLAS restatement of the reference) on `rows`
+    rows of the same workload; return seconds and thread count."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import bcgs_port
+    from bcgs_gb300 import inputs
+    X = inputs.graded_host(rows, args.n, args.kappa, seed=1)
+    t0 = time.perf_counter()
+    bcgs_port.run_variant(args.variant, X, args.n, args.s)
+    dt = time.perf_counter() - t0
+    return dt, os.cpu_count()
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    steps = []
+    for _ in range(max(0, args.warmup)):
+        pass  # one sample per step is already a few seconds of CPU work
+    threads = os.cpu_count()
+    for _ in range(max(1, args.steps)):
+        dt, threads = cpu_sample(args, args.cpu_rows)
+        steps.append(dt * args.m / args.cpu_rows * 1e3)
+    ms = sum(steps) / len(steps)
+    sample = (f"{args.variant} on {args.cpu_rows} rows x n={args.n}, s={args.s} (numpy/OpenBLAS "
+              f"restatement of the reference, {threads} threads), time scaled by m/{args.cpu_rows}")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms",
+        "n_gpus": args.gpus, "steps": len(steps), "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"{args.variant} QR m={args.m} n={args.n} s={args.s} "
+                               f"kappa={args.kappa:g}"},
+        "cpu_baseline": {"value": round(ms, 3), "unit": "ms", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(ms, 3), "unit": "ms", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+
+    from bcgs_gb300 import inputs, orth
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    orth.load()
+    m, n, s = args.m, args.n, args.s
+    variant = args.variant
+    split_ok = orth.split_supported(m, n, s) if hasattr(orth, "split_supported") else False
+    if args.precision == "fp64" or (args.precision == "auto" and not split_ok):
+        prec, prec_name = orth.FP64, "fp64"
+    else:
+        prec, prec_name = orth.SPLIT_BF16, "split_bf16"
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    X0 = inputs.graded_device(m, n, args.kappa, seed=1234 + rank, device=str(dev))  # (n, m)
+    X = torch.empty_like(X0)
+    R = torch.zeros((n, n), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    if orth.reserve(m, n, s) != 0:
+        raise RuntimeError("workspace reservation failed")
+
+    def one_qr(precision, timed_events=None):
+        with torch.cuda.stream(stream):
+            X.copy_(X0)
+            R.zero_()
+            if timed_events is not None:
+                timed_events[0].record(stream)
+            rc, _ = orth.run_dev(variant, m, n, s, X.data_ptr(), m, R.data_ptr(), n, precision,
+                                 sptr, want_status=False)
+            if timed_events is not None:
+                timed_events[1].record(stream)
+        if rc != 0:
+            raise RuntimeError(f"run_dev rc={rc}")
+
+    for _ in range(max(0, args.warmup)):
+        one_qr(prec)
+    torch.cuda.synchronize()
+    launches_per_qr = orth.last_launch_count()
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    orth.profile(True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            one_qr(prec, evs[k])
+        torch.cuda.synchronize()
+    barrier()
+    prof = orth.profile_read()
+    orth.profile(False)
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # Accuracy of the last timed QR (FP64 metrics, cuBLAS DGEMM on the device).
+    acc = {}
+    if not args.no_accuracy:
+        with torch.cuda.stream(stream):
+            Q = X.t()
+            G = Q.t() @ Q
+            G.diagonal().sub_(1.0)
+            acc["loo_2"] = float(torch.linalg.matrix_norm(G, ord=2).item())
+            acc["loo_fro"] = float(torch.linalg.matrix_norm(G).item())
+            del G
+            step = 1 << 20
+            num = 0.0
+            for r0 in range(0, m, step):
+                r1 = min(m, r0 + step)
+                blk = X0.t()[r0:r1] - Q[r0:r1] @ R.t()
+                num += float((blk * blk).sum().item())
+            den = float((X0 * X0).sum().item())
+            acc["rel_residual"] = (num / den) ** 0.5
+        torch.cuda.synchronize()
+
+    # FP64 reference leg beside a split-precision run.
+    fp64_ms = None
+    if prec != orth.FP64 and args.fp64_steps > 0:
+        one_qr(orth.FP64)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.fp64_steps)]
+        for k in range(args.fp64_steps):
+            one_qr(orth.FP64, ev[k])
+        torch.cuda.synchronize()
+        fp64_ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+
+    # End to end through the orth.h host entry point (pinned host buffers).
+    e2e = None
+    if not args.no_e2e and args.e2e_steps > 0:
+        import numpy as np
+        Xh_t = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
+        Rh_t = torch.zeros((n, n), dtype=torch.float64, pin_memory=True)
+        Xh = Xh_t.numpy().T          # m x n column-major view, ld = m
+        Rh = Rh_t.numpy().T
+        work = np.zeros(1)
+        times = []
+        for k in range(args.e2e_steps + 1):
+            Xh_t.copy_(X0, non_blocking=False)
+            Rh_t.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rc = orth.call(variant, m, n, s, Xh, m, Rh, n, work, orth.lwork_min(m, n, s, variant))
+            dt = time.perf_counter() - t0
+            if rc != 0:
+                raise RuntimeError(f"host entry point rc={rc}")
+            if k > 0:   # first call warms the host-path buffers
+                times.append(dt * 1e3)
+        e2e = {"value": round(sum(times) / len(times), 3), "unit": "ms",
+               "h2d_bytes_per_step": m * n * 8, "d2h_bytes_per_step": m * n * 8 + n * n * 8,
+               "path": "orth.h bcgsi2P1s (host pointers, pinned), FP64"}
+        del Xh_t, Rh_t
+
+    # Roofline of the dominant kernel class.
+    dom = max(("gram", "update"), key=lambda c: prof[c]["ms"])
+    pc = prof[dom]
+    launches = max(1, pc["launches"])
+    if prec == orth.FP64:
+        peak = orth.fp64_peak_tflops()
+        achieved = pc["flops"] / (pc["ms"] * 1e-3) / 1e12 if pc["ms"] > 0 else 0.0
+        roof = {"bound": "fp64", "achieved": round(achieved, 4), "peak": round(peak, 4),
+                "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
+                "traffic": None, "kernel": dom,
+                "peak_source": "live DFMA probe (orth_gb300_fp64_peak_probe); MEASURED_PEAKS.json has no FP64 figure",
+                "launch_ms": round(pc["ms"] / launches, 4)}
+    else:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
+            if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+        peak = peaks.get("bf16_tflops", 1900.0)
+        achieved = pc["flops"] / (pc["ms"] * 1e-3) / 1e12 if pc["ms"] > 0 else 0.0
+        roof = {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak, "unit": "TFLOP/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "kernel": dom}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        dt, threads = cpu_sample(args, args.cpu_rows)
+        cpu = {"value": round(dt * m / args.cpu_rows * 1e3, 3), "unit": "ms", "cores": threads,
+               "kind": "port",
+               "sample": f"{variant} on {args.cpu_rows} rows x n={n}, s={s} with the numpy/OpenBLAS "
+                         f"restatement of the reference; time scaled by m/{args.cpu_rows}"}
+
+    bytes_alg = alg_bytes_p1s(m, n, s)
+    flops_alg = alg_flops_p1s(m, n, s)
+    line = {
+        "metric": METRIC, "value": round(ms, 3), "unit": "ms", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"{variant} QR m={m} n={n} s={s} kappa={args.kappa:g} "
+                               f"(graded X = U diag(sigma) W^T)",
+                   "precision": prec_name, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs (34 GB) larger than L2; no flush",
+                   "restore": "X restored from a resident copy before each step, outside the timed interval"},
+        "hbm_gbs_alg": round(bytes_alg / (ms * 1e-3) / 1e9, 2),
+        "tflops_alg": round(flops_alg / (ms * 1e-3) / 1e12, 4),
+        "fp64_ms": round(fp64_ms, 3) if fp64_ms is not None else (round(ms, 3) if prec == orth.FP64 else None),
+        "accuracy": acc,
+        "gpu_launches": int(launches_per_qr * args.steps),
+        "kernel_profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"]} for k, v in prof.items()},
+        "roofline": roof,
+        "clocks": clk.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.gpus > 1 else "gloo")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,85 @@
+/*
+ * Extended C ABI of the GB300 BCGS library: device buffers, a caller stream,
+ * a precision mode and a status report. Plain pointers and sizes only.
+ *
+ * The reference has no counterpart for these entry points; each one runs the
+ * same algorithm as the same-named function of include/orth.h (reference
+ * include/orth.h:8-17) on buffers that already live on the GPU.
+ */
+#ifndef ORTH_GB300_H
+#define ORTH_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status of the last run. */
+typedef struct orth_gb300_status {
+    int breakdown_step;  /* 1-based block step of the first Cholesky breakdown, 0 if none */
+    int breakdown_info;  /* dpotrf-style info of that breakdown (1-based column) */
+    int timeout;         /* a bounded device wait gave up (no kernel here waits on a peer: 0) */
+    int cuda_error;      /* cudaError_t of the first failing CUDA call, 0 if none */
+} orth_gb300_status;
+
+/* Precision modes of the tall products (Q^T V and Q S). */
+#define ORTH_GB300_FP64 0        /* plain FP64 on the FP64 pipe */
+#define ORTH_GB300_SPLIT_BF16 1  /* split precision on the tensor cores */
+
+/* Variant identifiers for orth_gb300_run_dev. */
+#define ORTH_GB300_BCGSI2P1S 0
+#define ORTH_GB300_BCGSI21S 1
+#define ORTH_GB300_BCGSPIPI2 2
+#define ORTH_GB300_BCGSI2 3
+#define ORTH_GB300_BCGSI2P2S 4
+
+/*
+ * Device-pointer form of the orth.h entry points. dX: m x n column-major FP64
+ * on the current device, leading dimension ldX >= m, overwritten with Q.
+ * dR: n x n (ldR >= n) device buffer; the upper block triangle is written.
+ * stream: a cudaStream_t (NULL = legacy default stream). status: optional; when
+ * non-NULL the call waits for the stream and fills it, otherwise the call only
+ * enqueues work and returns.
+ * Return codes: 0 ok, 2 invalid arguments, 3 CUDA failure, 4 unsupported
+ * precision for this variant/shape.
+ */
+int orth_gb300_run_dev(int variant, int m, int n, int s, double *dX, long long ldX,
+                       double *dR, int ldR, int precision, void *stream,
+                       orth_gb300_status *status);
+
+/* Status of the last run through the orth.h entry points on this thread. */
+void orth_gb300_last_status(orth_gb300_status *status);
+
+/* Number of device-wide reductions ("synchronizations") a call performs. */
+int orth_gb300_sync_count(int variant, int n, int s);
+
+/* Number of kernel launches the last run enqueued (for launch accounting). */
+long long orth_gb300_last_launch_count(void);
+
+/*
+ * Per-kernel-class timing. orth_gb300_profile(1) resets the accumulators and
+ * records a CUDA event pair on the launching stream around every kernel group
+ * of later runs; orth_gb300_profile_read waits for them and returns, per class
+ * (0 tall Gram + reduction, 1 tall update, 2 small s x s kernels, 3 TSQR), the
+ * summed milliseconds, kernel launches, and algorithmic flops and bytes.
+ * Arrays have 4 entries; any may be NULL. Returns 0 or a cudaError_t.
+ */
+void orth_gb300_profile(int on);
+int orth_gb300_profile_read(double *ms, long long *launches, double *flops, double *bytes);
+
+/* Measure the FP64 pipe's throughput (TFLOP/s) with a DFMA loop; 0 or a cudaError_t. */
+int orth_gb300_fp64_peak_probe(double *tflops);
+
+/* Pre-size the cached device workspace for (m, n, s); 0 on success. */
+int orth_gb300_reserve(int m, int n, int s);
+
+/* Free the cached device workspace and staging buffers. */
+void orth_gb300_release(void);
+
+/* Library version string. */
+const char *orth_gb300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

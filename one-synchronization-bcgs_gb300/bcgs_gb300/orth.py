@@ -1,0 +1,182 @@
+"""Python binding of the GB300 BCGS C ABI (include/orth.h, include/orth_gb300.h).
+
+The five reference entry points keep their names and argument meanings
+(reference include/orth.h:8-17); they take numpy float64 arrays in Fortran order
+and call straight into ``liborth_gb300.so``. There is no fallback: if the
+library is missing or cannot load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+VARIANTS = ("bcgsi2P1s", "bcgsi21s", "bcgspipi2", "bcgsi2", "bcgsi2P2s")
+VARIANT_ID = {name: i for i, name in enumerate(VARIANTS)}
+FP64 = 0
+SPLIT_BF16 = 1
+
+
+class Status(ctypes.Structure):
+    _fields_ = [("breakdown_step", ctypes.c_int), ("breakdown_info", ctypes.c_int),
+                ("timeout", ctypes.c_int), ("cuda_error", ctypes.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(path: str | None = None):
+    """Load (once) and return the ctypes handle of liborth_gb300.so."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or _build.LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"liborth_gb300.so not built ({p}); run bcgs_gb300.build.build()")
+    lib = ctypes.CDLL(p)
+    dp = ctypes.POINTER(ctypes.c_double)
+    for name in VARIANTS:
+        f = getattr(lib, name)
+        f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, dp, ctypes.c_int,
+                      dp, ctypes.c_int]
+        f.restype = ctypes.c_int
+    lib.orth_gb300_run_dev.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.POINTER(Status)]
+    lib.orth_gb300_run_dev.restype = ctypes.c_int
+    lib.orth_gb300_last_status.argtypes = [ctypes.POINTER(Status)]
+    lib.orth_gb300_last_status.restype = None
+    lib.orth_gb300_sync_count.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.orth_gb300_sync_count.restype = ctypes.c_int
+    lib.orth_gb300_last_launch_count.argtypes = []
+    lib.orth_gb300_last_launch_count.restype = ctypes.c_longlong
+    lib.orth_gb300_profile.argtypes = [ctypes.c_int]
+    lib.orth_gb300_profile.restype = None
+    lib.orth_gb300_profile_read.argtypes = [ctypes.POINTER(ctypes.c_double),
+                                            ctypes.POINTER(ctypes.c_longlong),
+                                            ctypes.POINTER(ctypes.c_double),
+                                            ctypes.POINTER(ctypes.c_double)]
+    lib.orth_gb300_profile_read.restype = ctypes.c_int
+    lib.orth_gb300_fp64_peak_probe.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    lib.orth_gb300_fp64_peak_probe.restype = ctypes.c_int
+    lib.orth_gb300_reserve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.orth_gb300_reserve.restype = ctypes.c_int
+    lib.orth_gb300_release.argtypes = []
+    lib.orth_gb300_release.restype = None
+    lib.orth_gb300_version.argtypes = []
+    lib.orth_gb300_version.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def lwork_min(m: int, n: int, s: int, variant: str = "bcgsi2P1s") -> int:
+    """The reference's minimum lwork (SRC/orth.c:82, :489 for bcgsi2)."""
+    tall = m * s if variant == "bcgsi2" else m * n
+    return min(5 * n * s + 9 * s * s + tall, 2**31 - 1)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def call(variant: str, m: int, n: int, s: int, Xsub: np.ndarray, ldXsub: int, R: np.ndarray,
+         ldR: int, work: np.ndarray | None = None, lwork: int | None = None) -> int:
+    """Call the orth.h entry point ``variant`` exactly as C code would."""
+    lib = load()
+    if Xsub.dtype != np.float64 or R.dtype != np.float64:
+        raise TypeError("Xsub and R must be float64")
+    if lwork is None:
+        lwork = lwork_min(m, n, s, variant)
+    if work is None:
+        work = np.zeros(1)
+    return int(getattr(lib, variant)(m, n, s, _dp(Xsub), ldXsub, _dp(R), ldR, _dp(work), lwork))
+
+
+def qr(variant: str, X0: np.ndarray, s: int):
+    """Convenience: QR of a copy of X0 (m x n) through the orth.h entry point.
+
+    Returns (Q, R, rc, status_dict)."""
+    m, n = X0.shape
+    X = np.array(X0, dtype=np.float64, order="F", copy=True)
+    R = np.zeros((n, n), order="F")
+    rc = call(variant, m, n, s, X, m, R, n)
+    return X, R, rc, last_status()
+
+
+def last_status() -> dict:
+    st = Status()
+    load().orth_gb300_last_status(ctypes.byref(st))
+    return st.as_dict()
+
+
+def run_dev(variant: str, m: int, n: int, s: int, x_ptr: int, ldx: int, r_ptr: int, ldr: int,
+            precision: int = FP64, stream: int = 0, want_status: bool = True):
+    """Device-pointer entry point (orth_gb300_run_dev). Pointers are integers
+    (e.g. ``tensor.data_ptr()``); ``stream`` is a cudaStream_t as an integer."""
+    lib = load()
+    st = Status()
+    rc = lib.orth_gb300_run_dev(VARIANT_ID[variant], m, n, s, ctypes.c_void_p(x_ptr), ldx,
+                                ctypes.c_void_p(r_ptr), ldr, precision, ctypes.c_void_p(stream),
+                                ctypes.byref(st) if want_status else None)
+    return int(rc), (st.as_dict() if want_status else None)
+
+
+def sync_count(variant: str, n: int, s: int) -> int:
+    return int(load().orth_gb300_sync_count(VARIANT_ID[variant], n, s))
+
+
+def last_launch_count() -> int:
+    return int(load().orth_gb300_last_launch_count())
+
+
+PROFILE_CLASSES = ("gram", "update", "small", "tsqr")
+
+
+def profile(on: bool) -> None:
+    """Enable (and reset) or disable per-kernel-class event timing."""
+    load().orth_gb300_profile(1 if on else 0)
+
+
+def profile_read() -> dict:
+    """Per class: ms, launches, algorithmic flops and bytes since profile(True)."""
+    ms = (ctypes.c_double * 4)()
+    ln = (ctypes.c_longlong * 4)()
+    fl = (ctypes.c_double * 4)()
+    by = (ctypes.c_double * 4)()
+    rc = load().orth_gb300_profile_read(ms, ln, fl, by)
+    if rc != 0:
+        raise RuntimeError(f"orth_gb300_profile_read failed: {rc}")
+    return {c: {"ms": ms[i], "launches": ln[i], "flops": fl[i], "bytes": by[i]}
+            for i, c in enumerate(PROFILE_CLASSES)}
+
+
+def fp64_peak_tflops() -> float:
+    """FP64 pipe throughput of the current GPU, measured by a DFMA loop."""
+    v = ctypes.c_double(0.0)
+    rc = load().orth_gb300_fp64_peak_probe(ctypes.byref(v))
+    if rc != 0:
+        raise RuntimeError(f"fp64 probe failed: {rc}")
+    return float(v.value)
+
+
+def reserve(m: int, n: int, s: int) -> int:
+    return int(load().orth_gb300_reserve(m, n, s))
+
+
+def release() -> None:
+    load().orth_gb300_release()
+
+
+def version() -> str:
+    return load().orth_gb300_version().decode()

@@ -1,0 +1,40 @@
+// Internal launcher declarations shared by the kernel files and the C-ABI layer.
+// All matrices are column-major FP64 device buffers; every launcher enqueues on
+// `st` and returns a cudaError_t value (0 on success).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace bcgs {
+
+using i64 = long long;
+
+// Number of kernels enqueued by the launchers below since load (host counter).
+extern long long g_launch_count;
+
+// C (na x nb, ld ldo) = X[:, a0:a0+na]^T X[:, b0:b0+nb] over m rows, FP64, with a
+// fixed-order two-stage reduction through `part` (nchunks * na * nb doubles).
+int gram_chunks_fp64(i64 m, int na, int nb, int num_sms);
+int launch_gram_fp64(const double* X, i64 ld, i64 m, int a0, int na, int b0, int nb,
+                     double* out, int ldo, double* part, int nchunks, cudaStream_t st);
+
+// X[:, c0:c0+nc] = (X[:, c0:c0+nc] - X[:, q0:q0+K] S) T^{-1}; T upper (nc x nc) or null.
+int launch_update_fp64(double* X, i64 ld, i64 m, int q0, int K, int c0, int nc,
+                       const double* S, int lds, const double* T, int ldt, cudaStream_t st);
+
+// Small single-CTA kernels (nz, s, ny <= 64).
+int launch_pyth_chol(const double* Om, int ldom, const double* A, int lda, int k, int nz,
+                     double* T, int ldt, int* status, int step, cudaStream_t st);
+int launch_scol(const double* G, int ldg, int mZ, int s, int nZ, const double* Yd, int ldy,
+                double* Scol, int ldsc, cudaStream_t st);
+int launch_rblock(double* R, int ldR, int c0, int K, int ny, const double* A, int lda,
+                  const double* B, int ldb, const double* Sd, int ldsd, const double* Yd,
+                  int ldyd, int mode, cudaStream_t st);
+
+// Explicit TSQR of X[:, c0:c0+nc] in place; R (nc x nc, ldR) upper with diag >= 0.
+int tsqr_tile_rows(int nc);
+i64 tsqr_workspace_doubles(i64 m, int nc);
+int launch_tsqr(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR, double* ws,
+                cudaStream_t st);
+
+}  // namespace bcgs

@@ -1,0 +1,644 @@
+// C-ABI layer: the reference's include/orth.h entry points on one GB300, and the
+// device-pointer extension declared in include/orth_gb300.h.
+//
+// Each variant's driver below issues, per block step, exactly the reference's
+// sequence of operations (cited per line), with MPI_Allreduce replaced by one
+// deterministic device-wide reduction and every small s x s step kept on the
+// device, so a whole QR is enqueued on one stream with no host round trip.
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/orth.h"
+#include "../../include/orth_gb300.h"
+#include "common.cuh"
+#include "kernels.h"
+#include "split.h"
+
+namespace bcgs {
+
+long long g_launch_count = 0;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t want) {
+        if (want <= bytes) return 0;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) return (int)e;
+        bytes = want;
+        return 0;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+// Cached workspace (grow-only). The reference is not thread-safe either (it uses
+// MPI_COMM_WORLD collectives); calls are serialized by a mutex here.
+struct Context {
+    DevBuf part, gram, small, status, tsqr, hostX, hostR, split;
+    double* hostR_stage = nullptr;
+    size_t hostR_stage_bytes = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = kNumSMsDefault;
+    bool init = false;
+};
+
+Context g_ctx;
+std::mutex g_mu;
+
+// Optional per-kernel-class timing with CUDA events recorded on the launching
+// stream around each launch group. Classes: 0 tall Gram (incl. its reduction),
+// 1 tall update, 2 small s x s kernels, 3 TSQR.
+constexpr int kProfClasses = 4;
+struct ProfPending { int cls; cudaEvent_t a, b; };
+struct Prof {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    std::vector<ProfPending> pending;
+    double ms[kProfClasses] = {0, 0, 0, 0};
+    long long launches[kProfClasses] = {0, 0, 0, 0};
+    double flops[kProfClasses] = {0, 0, 0, 0};
+    double bytes[kProfClasses] = {0, 0, 0, 0};
+    cudaEvent_t get() {
+        if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+};
+Prof g_prof;
+
+struct ProfScope {
+    int cls;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr;
+    long long l0;
+    ProfScope(int c, cudaStream_t s, double flops, double bytes) : cls(c), st(s), l0(g_launch_count) {
+        if (!g_prof.on) return;
+        a = g_prof.get();
+        cudaEventRecord(a, st);
+        g_prof.flops[cls] += flops;
+        g_prof.bytes[cls] += bytes;
+    }
+    ~ProfScope() {
+        if (!g_prof.on) return;
+        cudaEvent_t b = g_prof.get();
+        cudaEventRecord(b, st);
+        g_prof.pending.push_back({cls, a, b});
+        g_prof.launches[cls] += g_launch_count - l0;
+    }
+};
+thread_local orth_gb300_status g_last_status = {0, 0, 0, 0};
+long long g_last_launches = 0;
+
+int init_ctx() {
+    if (g_ctx.init) return 0;
+    int dev = 0;
+    BCGS_CUDA_TRY(cudaGetDevice(&dev));
+    BCGS_CUDA_TRY(cudaDeviceGetAttribute(&g_ctx.num_sms, cudaDevAttrMultiProcessorCount, dev));
+    BCGS_CUDA_TRY(cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking));
+    g_ctx.init = true;
+    return 0;
+}
+
+// Largest Gram-partial buffer any step needs (doubles).
+i64 part_doubles(i64 m, int n, int s, int num_sms) {
+    i64 best = 0;
+    const int na_max = n + s, nb_max = 2 * s;
+    for (int na = 1; na <= na_max; ++na) {
+        for (int nb = 1; nb <= nb_max; ++nb) {
+            i64 v = gram_chunks_fp64(m, na, nb, num_sms) * (i64)na * nb;
+            if (v > best) best = v;
+        }
+    }
+    return best + 1024;
+}
+
+// Small buffers carved from one allocation (doubles).
+struct Small {
+    double* G1;    // (n+s) x 2s reduced Gram
+    double* G2;    // (n+s) x 2s second reduced Gram (two-sync variants)
+    double* Scol;  // n x s
+    double* S0;    // s x s first-step coefficients
+    double* Sd;    // s x s
+    double* Yd;    // s x s
+};
+
+i64 small_doubles(int n, int s) {
+    return 2LL * (n + s) * 2 * s + (i64)n * s + 3LL * s * s + 64;
+}
+
+Small carve_small(double* base, int n, int s) {
+    Small w;
+    w.G1 = base;
+    w.G2 = w.G1 + (i64)(n + s) * 2 * s;
+    w.Scol = w.G2 + (i64)(n + s) * 2 * s;
+    w.S0 = w.Scol + (i64)n * s;
+    w.Sd = w.S0 + (i64)s * s;
+    w.Yd = w.Sd + (i64)s * s;
+    return w;
+}
+
+int reserve(i64 m, int n, int s, int precision) {
+    int rc = init_ctx();
+    if (rc) return rc;
+    rc = g_ctx.part.ensure((size_t)part_doubles(m, n, s, g_ctx.num_sms) * sizeof(double));
+    if (rc) return rc;
+    rc = g_ctx.small.ensure((size_t)small_doubles(n, s) * sizeof(double));
+    if (rc) return rc;
+    rc = g_ctx.status.ensure(kStatusWords * sizeof(int));
+    if (rc) return rc;
+    rc = g_ctx.tsqr.ensure((size_t)tsqr_workspace_doubles(m, s) * sizeof(double));
+    if (rc) return rc;
+    if (precision == ORTH_GB300_SPLIT_BF16) {
+        rc = g_ctx.split.ensure((size_t)split_workspace_bytes(m, n, s, g_ctx.num_sms));
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Per-call engine: the primitives every variant is written in.
+// ---------------------------------------------------------------------------
+struct Engine {
+    double* X;
+    i64 ld;
+    i64 m;
+    int n, s;
+    double* R;
+    int ldR;
+    int precision;
+    cudaStream_t st;
+    Small w;
+    int* status;
+    int err = 0;
+
+    // C (na x nb, ld na) = X[:, 0:na]^T X[:, b0:b0+nb]: one synchronization.
+    void gram(int na, int b0, int nb, double* C) {
+        if (err || na <= 0 || nb <= 0) return;
+        ProfScope ps(0, st, 2.0 * m * na * nb, 8.0 * m * (na + nb));
+        if (precision == ORTH_GB300_SPLIT_BF16) {
+            err = launch_gram_split(X, ld, m, na, b0, nb, C, na, g_ctx.split.as<char>(),
+                                    g_ctx.split.bytes, g_ctx.num_sms, st);
+            return;
+        }
+        int chunks = gram_chunks_fp64(m, na, nb, g_ctx.num_sms);
+        err = launch_gram_fp64(X, ld, m, 0, na, b0, nb, C, na, g_ctx.part.as<double>(), chunks, st);
+    }
+    // X[:, c0:c0+nc] = (X[:, c0:c0+nc] - X[:, 0:K] S) T^{-1}
+    void update(int K, int c0, int nc, const double* S, int lds, const double* T, int ldt) {
+        if (err || nc <= 0) return;
+        ProfScope ps(1, st, 2.0 * m * K * nc + (T ? (double)m * nc * nc : 0.0),
+                     8.0 * m * (K + 2.0 * nc));
+        if (precision == ORTH_GB300_SPLIT_BF16) {
+            err = launch_update_split(X, ld, m, K, c0, nc, S, lds, T, ldt, g_ctx.split.as<char>(),
+                                      g_ctx.split.bytes, g_ctx.num_sms, st);
+            return;
+        }
+        err = launch_update_fp64(X, ld, m, 0, K, c0, nc, S, lds, T, ldt, st);
+    }
+    void pyth_chol(const double* Om, int ldom, const double* A, int lda, int k, int nz, double* T,
+                   int step) {
+        if (err) return;
+        ProfScope ps(2, st, 0.0, 0.0);
+        err = launch_pyth_chol(Om, ldom, A, lda, k, nz, T, nz, status, step, st);
+    }
+    void scol(const double* G, int ldg, int mZ, int nZ, const double* Yd, double* Scol) {
+        if (err) return;
+        ProfScope ps(2, st, 0.0, 0.0);
+        err = launch_scol(G, ldg, mZ, s, nZ, Yd, s, Scol, mZ + s, st);
+    }
+    void rblock(int c0, int K, int ny, const double* A, int lda, const double* B, int ldb,
+                const double* Sd, const double* Yd, int mode) {
+        if (err) return;
+        ProfScope ps(2, st, 0.0, 0.0);
+        err = launch_rblock(R, ldR, c0, K, ny, A, lda, B, ldb, Sd, ny, Yd, ny, mode, st);
+    }
+    // Explicit TSQR of X[:, c0:c0+nc]; R into (Rout, ldr).
+    void tsqr(int c0, int nc, double* Rout, int ldr) {
+        if (err) return;
+        ProfScope ps(3, st, 6.0 * m * nc * nc, 8.0 * m * nc * 3.0);
+        err = launch_tsqr(X, ld, m, c0, nc, Rout, ldr, g_ctx.tsqr.as<double>(), st);
+    }
+};
+
+int nblocks_after_first(int n, int s) { return (n - s + s - 1) / s; }  // p = ceil((n-s0)/s)
+
+// --------------------------- C1 bcgsi2P1s ----------------------------------
+// SRC/orth.c:48-222. One synchronization per block step.
+void run_p1s(Engine& e) {
+    const int s = e.s, n = e.n, s0 = s;
+    const int p = nblocks_after_first(n, s);
+    Small& w = e.w;
+    e.tsqr(0, s0, e.R, e.ldR);                                       // :105-107
+    // First step (:110-147).
+    double* W = w.G2;                                                // 2s x s, ld 2s
+    e.gram(2 * s, s0, s, W);                                         // :111-114
+    e.pyth_chol(W + s0, 2 * s, W, 2 * s, s0, s, w.Sd, 1);            // :115-119
+    e.update(s0, s0, s, W, 2 * s, w.Sd, s);                          // :121-124  U2
+    int nZ = n - s - s0 < s ? n - s - s0 : s;                        // :125
+    int na = 2 * s + nZ, nb = s + nZ;
+    double* G = w.G1;
+    e.gram(na, s0, nb, G);                                           // :127-133
+    e.pyth_chol(G + s0, na, G, na, s0, s, w.Yd, 1);                  // :134-137
+    e.update(s0, s0, s, G, na, w.Yd, s);                             // :139-142  Q2
+    e.rblock(s0, s0, s, W, 2 * s, G, na, w.Sd, w.Yd, 0);             // :144-147
+    int ldg = na;
+    int mZ = s0;
+    for (int i = 1; i < p; ++i) {                                    // :152-218
+        const int mScol = mZ + s;
+        e.scol(G, ldg, mZ, nZ, w.Yd, w.Scol);                        // :155-159
+        // Omega_k = X_k^T X_k from the last synchronization (:160-163).
+        e.pyth_chol(G + mScol + (i64)s * ldg, ldg, w.Scol, mScol, mScol, nZ, w.Sd, i + 1);  // :160-171
+        e.update(mScol, mScol, nZ, w.Scol, mScol, w.Sd, nZ);         // :173-176  U_k
+        int nY, nZn;
+        if (i < p - 1) {                                             // :177-190
+            nZn = n - (i + 1) * s - s0 < s ? n - (i + 1) * s - s0 : s;
+            na = mScol + s + nZn;
+            nb = s + nZn;
+            nY = s;
+        } else {                                                     // :191-199
+            nZn = nZ;
+            na = mScol + nZ;
+            nb = nZ;
+            nY = nZ;
+        }
+        e.gram(na, mScol, nb, G);                                    // the one sync
+        ldg = na;
+        e.pyth_chol(G + mScol, ldg, G, ldg, mScol, nY, w.Yd, i + 1); // :200-204
+        e.update(mScol, mScol, nY, G, ldg, w.Yd, nY);                // :206-209  Q_k
+        e.rblock(mScol, mScol, nY, w.Scol, mScol, G, ldg, w.Sd, w.Yd, 0);  // :211-215
+        mZ += s;
+        nZ = nZn;
+    }
+}
+
+// --------------------------- C2 bcgsi21s -----------------------------------
+// SRC/orth.c:224-367. One synchronization per block step; the first pass is an
+// unnormalized projection.
+void run_21s(Engine& e) {
+    const int s = e.s, n = e.n, s0 = s;
+    const int p = nblocks_after_first(n, s);
+    Small& w = e.w;
+    e.tsqr(0, s0, e.R, e.ldR);                                       // :269-271
+    e.gram(s0, s0, s, w.S0);                                         // :275-278
+    e.update(s0, s0, s, w.S0, s0, nullptr, 0);                       // :280-281
+    int nZ = n - s - s0 < s ? n - s - s0 : s;                        // :282
+    int na = 2 * s, nb = s + nZ;
+    double* G = w.G1;
+    e.gram(na, s0, nb, G);                                           // :284-287
+    e.pyth_chol(G + s0, na, G, na, s0, s, w.Yd, 1);                  // :288-291
+    e.update(s0, s0, s, G, na, w.Yd, s);                             // :293-296
+    e.rblock(s0, s0, s, w.S0, s0, G, na, nullptr, w.Yd, 1);          // :298-302
+    int ldg = na, mZ = s0;
+    for (int i = 1; i < p; ++i) {
+        const int mScol = mZ + s;
+        e.scol(G, ldg, mZ, nZ, w.Yd, w.Scol);                        // :310-314
+        e.update(mScol, mScol, nZ, w.Scol, mScol, nullptr, 0);       // :323-324
+        int nY, nZn;
+        if (i < p - 1) {                                             // :325-335
+            nZn = n - (i + 1) * s - s0 < s ? n - (i + 1) * s - s0 : s;
+            na = mScol + s;
+            nb = s + nZn;
+            nY = s;
+        } else {                                                     // :336-344
+            nZn = nZ;
+            na = mScol + nZ;
+            nb = nZ;
+            nY = nZ;
+        }
+        e.gram(na, mScol, nb, G);
+        ldg = na;
+        e.pyth_chol(G + mScol, ldg, G, ldg, mScol, nY, w.Yd, i + 1); // :345-349
+        e.update(mScol, mScol, nY, G, ldg, w.Yd, nY);                // :351-354
+        e.rblock(mScol, mScol, nY, w.Scol, mScol, G, ldg, nullptr, w.Yd, 1);  // :356-360
+        mZ += s;
+        nZ = nZn;
+    }
+}
+
+// --------------------------- C3 bcgspipi2 ----------------------------------
+// SRC/orth.c:369-462. Two synchronizations per block step.
+void run_pipi(Engine& e) {
+    const int s = e.s, n = e.n, s0 = s;
+    const int p = nblocks_after_first(n, s);
+    Small& w = e.w;
+    e.tsqr(0, s0, e.R, e.ldR);                                       // :411-413
+    int mScol = s0;
+    for (int i = 0; i < p; ++i) {
+        const int nZ = n - i * s - s0 < s ? n - i * s - s0 : s;       // :419
+        const int na = mScol + nZ;
+        e.gram(na, mScol, nZ, w.G1);                                 // :421-424
+        e.pyth_chol(w.G1 + mScol, na, w.G1, na, mScol, nZ, w.Sd, i + 1);  // :425-429
+        e.update(mScol, mScol, nZ, w.G1, na, w.Sd, nZ);              // :431-434
+        e.gram(na, mScol, nZ, w.G2);                                 // :435-438
+        e.pyth_chol(w.G2 + mScol, na, w.G2, na, mScol, nZ, w.Yd, i + 1);  // :440-444
+        e.update(mScol, mScol, nZ, w.G2, na, w.Yd, nZ);              // :446-449
+        e.rblock(mScol, mScol, nZ, w.G1, na, w.G2, na, w.Sd, w.Yd, 0);    // :451-455
+        mScol += s;
+    }
+}
+
+// --------------------------- C4 bcgsi2 -------------------------------------
+// SRC/orth.c:464-548. Two synchronizations and two TSQRs per block step.
+void run_bcgsi2(Engine& e) {
+    const int s = e.s, n = e.n, s0 = s;
+    const int p = nblocks_after_first(n, s);
+    Small& w = e.w;
+    e.tsqr(0, s0, e.R, e.ldR);                                       // :503-505
+    int mScol = s0;
+    for (int i = 0; i < p; ++i) {
+        const int nZ = n - i * s - s0 < s ? n - i * s - s0 : s;       // :511
+        e.gram(mScol, mScol, nZ, w.G1);                              // :512-515
+        e.update(mScol, mScol, nZ, w.G1, mScol, nullptr, 0);         // :518-519
+        e.tsqr(mScol, nZ, w.Sd, nZ);                                 // :520-523
+        e.gram(mScol, mScol, nZ, w.G2);                              // :524-527
+        e.update(mScol, mScol, nZ, w.G2, mScol, nullptr, 0);         // :530-531
+        e.tsqr(mScol, nZ, w.Yd, nZ);                                 // :532-535
+        e.rblock(mScol, mScol, nZ, w.G1, mScol, w.G2, mScol, w.Sd, w.Yd, 0);  // :537-541
+        mScol += s;
+    }
+}
+
+// --------------------------- C5 bcgsi2P2s ----------------------------------
+// SRC/orth.c:550-697. TSQR first pass, one Pythagorean synchronization.
+void run_p2s(Engine& e) {
+    const int s = e.s, n = e.n, s0 = s;
+    const int p = nblocks_after_first(n, s);
+    Small& w = e.w;
+    e.tsqr(0, s0, e.R, e.ldR);                                       // :599-601
+    e.gram(s0, s0, s, w.S0);                                         // :605-608
+    e.update(s0, s0, s, w.S0, s0, nullptr, 0);                       // :610-611
+    e.tsqr(s0, s, w.Sd, s);                                          // :612-614
+    int nZ = n - s - s0 < s ? n - s - s0 : s;                        // :615
+    int na = 2 * s, nb = s + nZ;
+    double* G = w.G1;
+    e.gram(na, s0, nb, G);                                           // :617-620
+    e.pyth_chol(G + s0, na, G, na, s0, s, w.Yd, 1);                  // :621-624
+    e.update(s0, s0, s, G, na, w.Yd, s);                             // :625-628
+    e.rblock(s0, s0, s, w.S0, s0, G, na, w.Sd, w.Yd, 0);             // :609,:630-633
+    int ldg = na, mZ = s0;
+    for (int i = 1; i < p; ++i) {
+        const int mScol = mZ + s;
+        e.scol(G, ldg, mZ, nZ, w.Yd, w.Scol);                        // :641-645
+        e.update(mScol, mScol, nZ, w.Scol, mScol, nullptr, 0);       // :647-648
+        e.tsqr(mScol, nZ, w.Sd, nZ);                                 // :649-652
+        int nY, nZn;
+        if (i < p - 1) {                                             // :653-666
+            nZn = n - (i + 1) * s - s0 < s ? n - (i + 1) * s - s0 : s;
+            na = mScol + s;          // X_{k+1}^T X_{k+1} (:660-662) is never used; skipped
+            nb = s + nZn;
+            nY = s;
+        } else {                                                     // :667-675
+            nZn = nZ;
+            na = mScol + nZ;
+            nb = nZ;
+            nY = nZ;
+        }
+        e.gram(na, mScol, nb, G);
+        ldg = na;
+        e.pyth_chol(G + mScol, ldg, G, ldg, mScol, nY, w.Yd, i + 1); // :676-680
+        e.update(mScol, mScol, nY, G, ldg, w.Yd, nY);                // :681-684
+        e.rblock(mScol, mScol, nY, w.Scol, mScol, G, ldg, w.Sd, w.Yd, 0);  // :686-690
+        mZ += s;
+        nZ = nZn;
+    }
+}
+
+bool valid_args(int m, int n, int s, long long ldX, int ldR) {
+    return m >= 1 && s >= 1 && s <= 64 && n >= 2 * s && ldX >= m && ldR >= n && (i64)m >= n;
+}
+
+int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR, int ldR,
+               int precision, cudaStream_t st, orth_gb300_status* out) {
+    if (!valid_args(m, n, s, ldX, ldR)) return 2;
+    if (variant < 0 || variant > 4) return 2;
+    if (precision != ORTH_GB300_FP64 && precision != ORTH_GB300_SPLIT_BF16) return 4;
+    if (precision == ORTH_GB300_SPLIT_BF16 && !split_supported(m, n, s)) return 4;
+    int rc = reserve(m, n, s, precision);
+    if (rc) {
+        if (out) { std::memset(out, 0, sizeof(*out)); out->cuda_error = rc; }
+        return 3;
+    }
+    const long long launches0 = g_launch_count;
+    Engine e{dX, (i64)ldX, (i64)m, n, s, dR, ldR, precision, st,
+             carve_small(g_ctx.small.as<double>(), n, s), g_ctx.status.as<int>()};
+    cudaError_t ce = cudaMemsetAsync(e.status, 0, kStatusWords * sizeof(int), st);
+    if (ce != cudaSuccess) e.err = (int)ce;
+    switch (variant) {
+        case ORTH_GB300_BCGSI2P1S: run_p1s(e); break;
+        case ORTH_GB300_BCGSI21S: run_21s(e); break;
+        case ORTH_GB300_BCGSPIPI2: run_pipi(e); break;
+        case ORTH_GB300_BCGSI2: run_bcgsi2(e); break;
+        default: run_p2s(e); break;
+    }
+    g_last_launches = g_launch_count - launches0;
+    if (out) {
+        std::memset(out, 0, sizeof(*out));
+        int h[kStatusWords] = {0, 0, 0, 0};
+        if (!e.err) {
+            ce = cudaMemcpyAsync(h, e.status, sizeof(h), cudaMemcpyDeviceToHost, st);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+            if (ce != cudaSuccess) e.err = (int)ce;
+        }
+        out->breakdown_step = h[0];
+        out->breakdown_info = h[1];
+        out->timeout = h[2];
+        out->cuda_error = e.err;
+    }
+    return e.err ? 3 : 0;
+}
+
+// Host-buffer form (the orth.h ABI).
+int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR,
+             double* work, int lwork, int precision) {
+    (void)work;
+    // lwork rule of the reference (SRC/orth.c:82,255,397,489,584), in 64 bits and
+    // capped at INT_MAX so that sizes the reference cannot index are still usable.
+    const i64 msub = m;
+    i64 need = 5LL * n * s + 9LL * s * s + (variant == ORTH_GB300_BCGSI2 ? msub * s : msub * n);
+    if (need > INT_MAX) need = INT_MAX;
+    if ((i64)lwork < need) {
+        printf("%% Work space is too small. It should be larger than 6*n*s + 8*s*s.\n");
+        fflush(stdout);
+        return 1;
+    }
+    if (!valid_args(m, n, s, ldXsub, ldR) || Xsub == nullptr || R == nullptr) return 2;
+    std::lock_guard<std::mutex> lock(g_mu);
+    int rc = init_ctx();
+    if (rc) return 3;
+    cudaStream_t st = g_ctx.stream;
+    const size_t xbytes = (size_t)m * n * sizeof(double);
+    const size_t rbytes = (size_t)n * n * sizeof(double);
+    if (g_ctx.hostX.ensure(xbytes) || g_ctx.hostR.ensure(rbytes)) return 3;
+    if (g_ctx.hostR_stage_bytes < rbytes) {
+        if (g_ctx.hostR_stage) cudaFreeHost(g_ctx.hostR_stage);
+        g_ctx.hostR_stage = nullptr;
+        g_ctx.hostR_stage_bytes = 0;
+        if (cudaMallocHost(&g_ctx.hostR_stage, rbytes) != cudaSuccess) return 3;
+        g_ctx.hostR_stage_bytes = rbytes;
+    }
+    double* dX = g_ctx.hostX.as<double>();
+    double* dR = g_ctx.hostR.as<double>();
+    orth_gb300_status stt;
+    std::memset(&stt, 0, sizeof(stt));
+    cudaError_t ce = cudaMemcpy2DAsync(dX, (size_t)m * sizeof(double), Xsub,
+                                       (size_t)ldXsub * sizeof(double), (size_t)m * sizeof(double),
+                                       (size_t)n, cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(dR, 0, rbytes, st);
+    if (ce != cudaSuccess) {
+        stt.cuda_error = (int)ce;
+        g_last_status = stt;
+        return 3;
+    }
+    rc = run_device(variant, m, n, s, dX, m, dR, n, precision, st, &stt);
+    if (rc) {
+        g_last_status = stt;
+        return rc;
+    }
+    ce = cudaMemcpy2DAsync(Xsub, (size_t)ldXsub * sizeof(double), dX, (size_t)m * sizeof(double),
+                           (size_t)m * sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(g_ctx.hostR_stage, dR, rbytes, cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) {
+        stt.cuda_error = (int)ce;
+        g_last_status = stt;
+        return 3;
+    }
+    // Write back what the reference writes: for column j of block b, rows
+    // [0, end of block b); bcgsi21s writes only the upper triangle of its
+    // diagonal blocks after the first (SRC/orth.c:302,360 use dlacpy 'U').
+    const double* hs = g_ctx.hostR_stage;
+    for (int j = 0; j < n; ++j) {
+        const int b = j / s;
+        int rows = (b + 1) * s < n ? (b + 1) * s : n;
+        if (variant == ORTH_GB300_BCGSI21S && b >= 1) rows = j + 1;
+        std::memcpy(R + (size_t)j * ldR, hs + (size_t)j * n, (size_t)rows * sizeof(double));
+    }
+    g_last_status = stt;
+    return 0;
+}
+
+}  // namespace
+}  // namespace bcgs
+
+using namespace bcgs;
+
+extern "C" {
+
+int bcgsi2P1s(int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR, double* work,
+              int lwork) {
+    return run_host(ORTH_GB300_BCGSI2P1S, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, ORTH_GB300_FP64);
+}
+int bcgsi21s(int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR, double* work,
+             int lwork) {
+    return run_host(ORTH_GB300_BCGSI21S, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, ORTH_GB300_FP64);
+}
+int bcgspipi2(int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR, double* work,
+              int lwork) {
+    return run_host(ORTH_GB300_BCGSPIPI2, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, ORTH_GB300_FP64);
+}
+int bcgsi2(int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR, double* work,
+           int lwork) {
+    return run_host(ORTH_GB300_BCGSI2, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, ORTH_GB300_FP64);
+}
+int bcgsi2P2s(int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR, double* work,
+              int lwork) {
+    return run_host(ORTH_GB300_BCGSI2P2S, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, ORTH_GB300_FP64);
+}
+
+int orth_gb300_run_dev(int variant, int m, int n, int s, double* dX, long long ldX, double* dR,
+                       int ldR, int precision, void* stream, orth_gb300_status* status) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    return run_device(variant, m, n, s, dX, ldX, dR, ldR, precision, (cudaStream_t)stream, status);
+}
+
+void orth_gb300_last_status(orth_gb300_status* status) {
+    if (status) *status = g_last_status;
+}
+
+int orth_gb300_sync_count(int variant, int n, int s) {
+    if (s < 1 || n < 2 * s) return -1;
+    const int p = nblocks_after_first(n, s);
+    switch (variant) {
+        case ORTH_GB300_BCGSI2P1S: return 2 + (p - 1);   // first step 2, then 1 per step
+        case ORTH_GB300_BCGSI21S: return 2 + (p - 1);
+        case ORTH_GB300_BCGSPIPI2: return 2 * p;
+        case ORTH_GB300_BCGSI2: return 2 * p;
+        case ORTH_GB300_BCGSI2P2S: return 2 + (p - 1);
+        default: return -1;
+    }
+}
+
+long long orth_gb300_last_launch_count(void) { return g_last_launches; }
+
+void orth_gb300_profile(int on) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    for (auto& p : g_prof.pending) { g_prof.pool.push_back(p.a); g_prof.pool.push_back(p.b); }
+    g_prof.pending.clear();
+    for (int c = 0; c < kProfClasses; ++c) {
+        g_prof.ms[c] = 0; g_prof.launches[c] = 0; g_prof.flops[c] = 0; g_prof.bytes[c] = 0;
+    }
+    g_prof.on = on != 0;
+}
+
+int orth_gb300_profile_read(double* ms, long long* launches, double* flops, double* bytes) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    for (auto& p : g_prof.pending) {
+        float e = 0.f;
+        cudaError_t ce = cudaEventSynchronize(p.b);
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&e, p.a, p.b);
+        if (ce != cudaSuccess) return (int)ce;
+        g_prof.ms[p.cls] += e;
+        g_prof.pool.push_back(p.a);
+        g_prof.pool.push_back(p.b);
+    }
+    g_prof.pending.clear();
+    for (int c = 0; c < kProfClasses; ++c) {
+        if (ms) ms[c] = g_prof.ms[c];
+        if (launches) launches[c] = g_prof.launches[c];
+        if (flops) flops[c] = g_prof.flops[c];
+        if (bytes) bytes[c] = g_prof.bytes[c];
+    }
+    return 0;
+}
+
+int orth_gb300_reserve(int m, int n, int s) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (!valid_args(m, n, s, m, n)) return 2;
+    int rc = reserve(m, n, s, split_supported(m, n, s) ? ORTH_GB300_SPLIT_BF16 : ORTH_GB300_FP64);
+    return rc ? 3 : 0;
+}
+
+void orth_gb300_release(void) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    g_ctx.part.release();
+    g_ctx.gram.release();
+    g_ctx.small.release();
+    g_ctx.status.release();
+    g_ctx.tsqr.release();
+    g_ctx.hostX.release();
+    g_ctx.hostR.release();
+    g_ctx.split.release();
+    if (g_ctx.hostR_stage) cudaFreeHost(g_ctx.hostR_stage);
+    g_ctx.hostR_stage = nullptr;
+    g_ctx.hostR_stage_bytes = 0;
+}
+
+const char* orth_gb300_version(void) { return "orth_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

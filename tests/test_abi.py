@@ -1,0 +1,67 @@
+"""CPU tests of the C-ABI library: it builds, loads, exports every declared
+entry point, and applies the reference's argument checks before touching a GPU."""
+import os
+import re
+import subprocess
+
+import numpy as np
+
+from bcgs_gb300 import orth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in ("orth.h", "orth_gb300.h"):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:int|void|long long|const char\s*\*)\s*\**\s*(\w+)\s*\(", text, re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", orth.lib_path()], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    declared = declared_functions()
+    assert {"bcgsi2P1s", "bcgsi21s", "bcgspipi2", "bcgsi2", "bcgsi2P2s"} <= declared
+    missing = declared - exported
+    assert not missing, missing
+
+
+def test_lwork_too_small_returns_1(lib, capfd):
+    m, n, s = 64, 16, 4
+    X = np.zeros((m, n), order="F")
+    R = np.zeros((n, n), order="F")
+    for v in orth.VARIANTS:
+        need = orth.lwork_min(m, n, s, v)
+        rc = orth.call(v, m, n, s, X, m, R, n, lwork=need - 1)
+        assert rc == 1
+    assert "Work space is too small" in capfd.readouterr().out
+
+
+def test_invalid_arguments_return_2(lib):
+    X = np.zeros((64, 16), order="F")
+    R = np.zeros((16, 16), order="F")
+    assert orth.call("bcgsi2P1s", 64, 16, 9, X, 64, R, 16) == 2      # n < 2s
+    assert orth.call("bcgsi2P1s", 64, 16, 4, X, 63, R, 16) == 2      # ld < m
+    assert orth.call("bcgsi2P1s", 64, 16, 4, X, 64, R, 15) == 2      # ldR < n
+    assert orth.call("bcgsi2P1s", 64, 16, 0, X, 64, R, 16) == 2      # s < 1
+
+
+def test_sync_counts(lib):
+    # BCGSI+P-1S / BCGSI+A-1S / BCGSI+P-2S: two synchronizations in the first
+    # step, then exactly one per block step; PIPI and BCGSI+ two per step.
+    n, s = 512, 16
+    p = (n - s + s - 1) // s
+    assert orth.sync_count("bcgsi2P1s", n, s) == p + 1
+    assert orth.sync_count("bcgsi21s", n, s) == p + 1
+    assert orth.sync_count("bcgsi2P2s", n, s) == p + 1
+    assert orth.sync_count("bcgspipi2", n, s) == 2 * p
+    assert orth.sync_count("bcgsi2", n, s) == 2 * p
+
+
+def test_version(lib):
+    assert "sm_103a" in orth.version()

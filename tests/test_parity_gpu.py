@@ -1,0 +1,152 @@
+"""GPU parity tests: the CUDA path through the C ABI against the oracle.
+
+Every test calls liborth_gb300.so through ctypes (the orth.h entry points or the
+device-pointer entry point). The oracle is the reference's own output (golden
+fixtures made by oracle/_ref) and the numpy restatement (oracle/bcgs_port.py).
+Tolerances: Q and R/||R|| entries within 200*u*cond(X) + 1e-13 after sign
+normalization; LOO and relative residual within 10x of the reference's (with an
+n*u floor), the spec parity rule.
+"""
+import numpy as np
+import pytest
+
+import bcgs_port as port
+from bcgs_gb300 import inputs, orth
+from helpers import U, VARIANTS, load_golden, metric_ok, qr_tolerance, sign_normalize
+
+pytestmark = pytest.mark.gpu
+GOLD = load_golden()
+
+
+def _compare(X, Q, R, Qref, Rref, cond):
+    Qs, Rs = sign_normalize(Q, R)
+    Qr, Rr = sign_normalize(Qref, Rref)
+    tol = qr_tolerance(cond)
+    assert np.max(np.abs(Rs - Rr)) <= tol * np.max(np.abs(Rr))
+    assert np.max(np.abs(Qs - Qr)) <= tol
+
+
+@pytest.mark.parametrize("case", sorted(GOLD))
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_golden_fp64(lib, case, variant):
+    g = GOLD[case]
+    X, n, s = g["X"], g["n"], g["s"]
+    gv = g[variant]
+    Q, R, rc, st = orth.qr(variant, X, s)
+    assert rc == 0 and st["cuda_error"] == 0
+    if gv["info"] != 0:
+        if case == "edge_n2s_plus4" and variant == "bcgsi2P1s":
+            # The reference reads its first-step X_3^T X_3 buffer with the wrong
+            # leading dimension when 2s < n < 3s (SRC/orth.c:129-131 vs :160-163),
+            # which breaks its Cholesky. This library forms the intended Omega:
+            # no breakdown, and a Q at least as orthogonal as the reference's.
+            assert st["breakdown_step"] == 0
+            assert port.loo_fro(Q) <= gv["metrics"][0]
+            assert port.rel_residual(X, Q, R) <= 10 * max(gv["metrics"][2], n * U)
+        else:
+            # Both break down. Near breakdown the first failing step depends on
+            # rounding (the Gram sums are ordered differently from OpenBLAS), so
+            # ours may fail one step earlier or later than the reference.
+            assert st["breakdown_step"] > 0
+            assert abs(st["breakdown_step"] - gv["info"]) <= 1
+        return
+    assert st["breakdown_step"] == 0
+    Rg = gv["R"]
+    d = np.sign(np.diag(Rg)).copy()
+    d[d == 0] = 1
+    tol = qr_tolerance(g["cond"])
+    Qs, Rs = sign_normalize(Q, R)
+    assert np.max(np.abs(Rs - Rg * d[:, None])) <= tol * np.max(np.abs(Rg))
+    assert np.max(np.abs(Qs[:: g["qstride"], :] - gv["Qrows"] * d)) <= tol
+    loo_f, _, res = gv["metrics"]
+    assert metric_ok(port.loo_fro(Q), loo_f, n * U)
+    assert metric_ok(port.rel_residual(X, Q, R), res, n * U)
+
+
+@pytest.mark.parametrize("shape", [(3000, 50, 7), (2048, 10, 1), (4096, 128, 32), (6000, 128, 64),
+                                   (1000, 37, 16), (777, 24, 12)])
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_random_shapes_vs_oracle(lib, shape, variant):
+    m, n, s = shape
+    X = inputs.graded_host(m, n, 1e4, seed=m + n + s)
+    Q, R, rc, st = orth.qr(variant, X, s)
+    assert rc == 0 and st["breakdown_step"] == 0
+    Qp, Rp, info = port.run_variant(variant, X, n, s)
+    if variant == "bcgsi2P1s" and 2 * s < n < 3 * s:
+        # The reference's leading-dimension quirk (SRC/orth.c:129-131 vs
+        # :160-163), reproduced by the oracle, perturbs its first loop step;
+        # this library forms the intended Omega. Compare accuracy only.
+        assert port.loo_fro(Q) <= max(port.loo_fro(Qp), n * U)
+        assert metric_ok(port.rel_residual(X, Q, R), port.rel_residual(X, Qp, Rp), n * U)
+        return
+    assert info == 0
+    _compare(X, Q, R, Qp, Rp, 1e4)
+    assert metric_ok(port.loo_fro(Q), port.loo_fro(Qp), n * U)
+    assert metric_ok(port.rel_residual(X, Q, R), port.rel_residual(X, Qp, Rp), n * U)
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_bit_exact_run_to_run(lib, variant):
+    X = inputs.graded_host(20000, 96, 1e6, seed=42)
+    Q1, R1, rc1, _ = orth.qr(variant, X, 16)
+    Q2, R2, rc2, _ = orth.qr(variant, X, 16)
+    assert rc1 == rc2 == 0
+    assert np.array_equal(Q1, Q2) and np.array_equal(R1, R2)
+
+
+def test_leading_dimension_and_untouched_lower_blocks(lib):
+    m, n, s, ldx = 1500, 40, 8, 1600
+    X = inputs.graded_host(m, n, 1e3, seed=9)
+    Xb = np.full((ldx, n), 7.0, order="F")
+    Xb[:m, :] = X
+    R = np.full((n, n), -3.0, order="F")
+    rc = orth.call("bcgsi2P1s", m, n, s, Xb, ldx, R, n)
+    assert rc == 0
+    assert np.all(Xb[m:, :] == 7.0)                 # rows past m untouched
+    for j in range(n):                              # lower block triangle untouched
+        b = j // s
+        assert np.all(R[(b + 1) * s:, j] == -3.0)
+    Qp, Rp, _ = port.run_variant("bcgsi2P1s", X, n, s)
+    Rm = R.copy()
+    for j in range(n):
+        Rm[(j // s + 1) * s:, j] = 0.0
+    _compare(X, Xb[:m, :], Rm, Qp, Rp, 1e3)
+
+
+def test_device_entry_point_matches_host(lib):
+    torch = pytest.importorskip("torch")
+    m, n, s = 50000, 64, 16
+    X = inputs.graded_host(m, n, 1e5, seed=3)
+    Qh, Rh, rc, _ = orth.qr("bcgsi2P1s", X, s)
+    assert rc == 0
+    dX = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()      # (n, m) row-major == X col-major
+    dR = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    rc, st = orth.run_dev("bcgsi2P1s", m, n, s, dX.data_ptr(), m, dR.data_ptr(), n,
+                          orth.FP64, stream)
+    assert rc == 0 and st["breakdown_step"] == 0
+    Qd = dX.cpu().numpy().T
+    Rd = dR.cpu().numpy().T
+    assert np.array_equal(Qd, Qh)
+    assert np.array_equal(np.triu(Rd), np.triu(Rh))
+
+
+def test_large_properties_fp64(lib):
+    """Size-independent properties at m = 2^20: orthogonality and residual."""
+    torch = pytest.importorskip("torch")
+    m, n, s = 1 << 20, 256, 16
+    Xt = inputs.graded_device(m, n, 1e6, seed=5)          # (n, m) == X column-major
+    X0 = Xt.clone()
+    for variant in VARIANTS:
+        Xt.copy_(X0)
+        R = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        rc, st = orth.run_dev(variant, m, n, s, Xt.data_ptr(), m, R.data_ptr(), n, orth.FP64,
+                              torch.cuda.current_stream().cuda_stream)
+        assert rc == 0 and st["breakdown_step"] == 0, (variant, st)
+        Q = Xt.t()
+        Rm = R.t()
+        G = Q.t() @ Q - torch.eye(n, dtype=torch.float64, device="cuda")
+        loo = torch.linalg.matrix_norm(G, ord=2).item()
+        res = (torch.linalg.matrix_norm(X0.t() - Q @ Rm) / torch.linalg.matrix_norm(X0.t())).item()
+        assert loo < 1e-12, (variant, loo)
+        assert res < 1e-14, (variant, res)
