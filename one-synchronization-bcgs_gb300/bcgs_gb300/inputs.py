@@ -60,27 +60,36 @@ def _torch():
 
 
 def graded_device(m: int, n: int, kappa: float, seed: int = 0, device: str = "cuda:0"):
-    """Device version of ``graded_host``: returns a column-major torch tensor
-    (shape (n, m) row-major storage == m x n column-major, ld = m)."""
+    """Device version of ``graded_host``: returns a torch tensor of shape (n, m)
+    whose row-major storage is X column-major (ld = m).
+
+    U is the Q factor of the seeded Gaussian G, formed by two rounds of
+    Cholesky QR (a Gaussian m x n matrix with m >> n is well conditioned, so two
+    rounds give orthonormality to rounding). Only the tall products run on the
+    GPU (matmul); the n x n factorizations run on the host with numpy, so this
+    needs no GPU linear-algebra library.
+    """
     torch = _torch()
     g = torch.Generator(device=device)
     g.manual_seed(seed)
-    # Column-major m x n == row-major n x m; QR of the m x n matrix through the
-    # transpose view keeps the storage column-major.
-    Gt = torch.randn((n, m), generator=g, device=device, dtype=torch.float64)
-    U = torch.linalg.qr(Gt.t(), mode="reduced")[0]          # m x n
-    del Gt
-    Wg = torch.randn((n, n), generator=g, device=device, dtype=torch.float64)
-    W = torch.linalg.qr(Wg, mode="reduced")[0]
-    sigma = torch.logspace(0.0, -float(np.log10(kappa)), n, device=device, dtype=torch.float64)
-    M = (W * sigma).t()                                        # diag(sigma) W^T, n x n
+    Ut = torch.randn((n, m), generator=g, device=device, dtype=torch.float64)   # U^T, row-major
+    for _ in range(2):
+        Gram = (Ut @ Ut.t()).cpu().numpy()
+        L = np.linalg.cholesky(0.5 * (Gram + Gram.T))
+        Linv = torch.from_numpy(np.linalg.inv(L)).to(device)
+        Ut = Linv @ Ut                       # (L^{-1} U^T) == (U L^{-T})^T
+    rng = np.random.default_rng(seed + 1)
+    W, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    sigma = np.logspace(0.0, -np.log10(kappa), n) if n > 1 else np.ones(1)
+    M = torch.from_numpy(np.ascontiguousarray((W * sigma).T)).to(device)   # diag(sigma) W^T
+    # X^T = M^T U^T, written in row blocks of X (column blocks of X^T).
     Xt = torch.empty((n, m), device=device, dtype=torch.float64)
-    # X = U M; store X^T row-major, i.e. X column-major.
     step = 1 << 20
+    Mt = M.t().contiguous()
     for r0 in range(0, m, step):
         r1 = min(m, r0 + step)
-        Xt[:, r0:r1] = (U[r0:r1, :] @ M).t()
-    del U
+        Xt[:, r0:r1] = Mt @ Ut[:, r0:r1]
+    del Ut
     return Xt
 
 
@@ -93,11 +102,11 @@ def monomial_device(m: int, n: int, s: int, seed: int = 0, device: str = "cuda:0
     Xt = torch.empty((n, m), device=device, dtype=torch.float64)
     j = 0
     while j < n:
-        w = v / torch.linalg.vector_norm(v)
+        w = v / torch.sqrt((v * v).sum())
         for i in range(min(s, n - j)):
             Xt[j + i] = w
             w = a * w
-            w = w / torch.linalg.vector_norm(w)
+            w = w / torch.sqrt((w * w).sum())
         v = Xt[j + min(s, n - j) - 1].clone()
         j += s
     return Xt
