@@ -46,6 +46,24 @@ int orth_gb300_run_dev(int variant, int m, int n, int s, double *dX, long long l
                        double *dR, int ldR, int precision, void *stream,
                        orth_gb300_status *status);
 
+/*
+ * BCGSI+P-1S on device buffers without allocating. There is no counterpart in
+ * the reference. It is for callers that cannot call cudaMalloc: code running
+ * inside another framework's memory pool or allocator callback, and embedded or
+ * real-time programs whose device memory is fixed at start-up. Arguments and
+ * results are those of orth_gb300_run_dev(ORTH_GB300_BCGSI2P1S, ..., FP64).
+ * All scratch comes from one 16 MiB array held by the library on every GPU
+ * that loads it (for example m up to 2^19 with n <= 512, s <= 16 fits); larger
+ * shapes return ORTH_GB300_NOALLOC_TOO_LARGE with a message on stderr. Calls
+ * share that array: calls that overlap on the GPU race, so issue them one after
+ * another. The first call on a device resolves the array's device address; make
+ * it before any stream capture.
+ */
+#define ORTH_GB300_NOALLOC_TOO_LARGE 5
+int orth_gb300_bcgsi2P1s_dev_noalloc(int m, int n, int s, double *dX, long long ldX,
+                                     double *dR, int ldR, void *stream,
+                                     orth_gb300_status *status);
+
 /* Status of the last run through the orth.h entry points on this thread. */
 void orth_gb300_last_status(orth_gb300_status *status);
 

@@ -70,6 +70,10 @@ def load(path: str | None = None):
     lib.orth_gb300_profile_read.restype = ctypes.c_int
     lib.orth_gb300_fp64_peak_probe.argtypes = [ctypes.POINTER(ctypes.c_double)]
     lib.orth_gb300_fp64_peak_probe.restype = ctypes.c_int
+    lib.orth_gb300_bcgsi2P1s_dev_noalloc.argtypes = [
+        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong,
+        ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(Status)]
+    lib.orth_gb300_bcgsi2P1s_dev_noalloc.restype = ctypes.c_int
     lib.orth_gb300_reserve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.orth_gb300_reserve.restype = ctypes.c_int
     lib.orth_gb300_release.argtypes = []
@@ -130,6 +134,20 @@ def run_dev(variant: str, m: int, n: int, s: int, x_ptr: int, ldx: int, r_ptr: i
                                 ctypes.c_void_p(r_ptr), ldr, precision, ctypes.c_void_p(stream),
                                 ctypes.byref(st) if want_status else None)
     return int(rc), (st.as_dict() if want_status else None)
+
+
+NOALLOC_TOO_LARGE = 5
+
+
+def bcgsi2P1s_dev_noalloc(m: int, n: int, s: int, x_ptr: int, ldx: int, r_ptr: int, ldr: int,
+                          stream: int = 0):
+    """BCGSI+P-1S on device buffers with no device allocation (scratch lives in
+    a fixed 16 MiB array inside the library). Returns (rc, status dict)."""
+    st = Status()
+    rc = load().orth_gb300_bcgsi2P1s_dev_noalloc(m, n, s, ctypes.c_void_p(x_ptr), ldx,
+                                                 ctypes.c_void_p(r_ptr), ldr,
+                                                 ctypes.c_void_p(stream), ctypes.byref(st))
+    return int(rc), st.as_dict()
 
 
 def sync_count(variant: str, n: int, s: int) -> int:
