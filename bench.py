@@ -34,7 +34,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "one-synchronization-bcgs_gb300"))
 
-METRIC = "ms per BCGSI+P-1S QR (m=2^23, n=512, s=16, FP64 in/out)"
+METRIC = "ms per BCGSI+P-1S QR (m=2^23, n=512, s=16, FP64 in/out, LOO<=1e-12)"
 
 
 def parse():
@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--precision", choices=["auto", "fp64", "split"], default="auto")
     ap.add_argument("--fp64-steps", type=int, default=1,
                     help="timed FP64 QRs reported beside a split-precision run")
+    ap.add_argument("--fast-steps", type=int, default=1,
+                    help="timed 48-bit split QRs reported beside the 56-bit split run")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-rows", type=int, default=1 << 19,
                     help="rows of the bounded CPU sample (time scaled to m)")
@@ -136,6 +138,18 @@ def alg_flops_p1s(m: int, n: int, s: int) -> float:
     return 4.0 * m * n * n + 8.0 * m * n * s
 
 
+def traffic_from_profiles(kernel_class: str):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary
+    (profiles/traffic.json), or None when no capture has been summarized."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    try:
+        return json.load(open(p)).get(kernel_class)
+    except Exception:
+        return None
+
+
 def cpu_sample(args, rows: int):
     """Time the oracle (numpy/OpenBLAS restatement of the reference) on `rows`
     rows of the same workload; return seconds and thread count."""
@@ -188,11 +202,11 @@ def run_ours(args, rank, world, local_rank):
     orth.load()
     m, n, s = args.m, args.n, args.s
     variant = args.variant
-    split_ok = orth.split_supported(m, n, s) if hasattr(orth, "split_supported") else False
+    split_ok = orth.split_supported(m, n, s)
     if args.precision == "fp64" or (args.precision == "auto" and not split_ok):
         prec, prec_name = orth.FP64, "fp64"
     else:
-        prec, prec_name = orth.SPLIT_BF16, "split_bf16"
+        prec, prec_name = orth.SPLIT_BF16, "split_bf16x7 (56-bit digit planes on tcgen05)"
 
     def barrier():
         if world > 1:
@@ -243,9 +257,9 @@ def run_ours(args, rank, world, local_rank):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
 
-    # Accuracy of the last timed QR (FP64 metrics, cuBLAS DGEMM on the device).
-    acc = {}
-    if not args.no_accuracy:
+    # Accuracy of a finished QR (FP64 metrics, cuBLAS DGEMM on the device).
+    def accuracy():
+        acc = {}
         with torch.cuda.stream(stream):
             Q = X.t()
             G = Q.t() @ Q
@@ -265,17 +279,26 @@ def run_ours(args, rank, world, local_rank):
             den = float((X0 * X0).sum().item())
             acc["rel_residual"] = (num / den) ** 0.5
         torch.cuda.synchronize()
+        return acc
 
-    # FP64 reference leg beside a split-precision run.
-    fp64_ms = None
-    if prec != orth.FP64 and args.fp64_steps > 0:
-        one_qr(orth.FP64)
+    acc = {} if args.no_accuracy else accuracy()
+
+    def side_leg(precision, steps):
+        one_qr(precision)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-              for _ in range(args.fp64_steps)]
-        for k in range(args.fp64_steps):
-            one_qr(orth.FP64, ev[k])
+              for _ in range(steps)]
+        for k in range(steps):
+            one_qr(precision, ev[k])
         torch.cuda.synchronize()
-        fp64_ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+        ms_ = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+        return ms_, ({} if args.no_accuracy else accuracy())
+
+    # FP64 leg and 48-bit split leg beside the 56-bit split run.
+    fp64_ms = fp64_acc = fast_ms = fast_acc = None
+    if prec != orth.FP64 and args.fp64_steps > 0:
+        fp64_ms, fp64_acc = side_leg(orth.FP64, args.fp64_steps)
+    if prec != orth.FP64 and args.fast_steps > 0:
+        fast_ms, fast_acc = side_leg(orth.SPLIT_BF16_FAST, args.fast_steps)
 
     # End to end through the orth.h host entry point (pinned host buffers).
     e2e = None
@@ -286,6 +309,7 @@ def run_ours(args, rank, world, local_rank):
         Xh = Xh_t.numpy().T          # m x n column-major view, ld = m
         Rh = Rh_t.numpy().T
         work = np.zeros(1)
+        orth.set_host_precision(prec)
         times = []
         for k in range(args.e2e_steps + 1):
             Xh_t.copy_(X0, non_blocking=False)
@@ -300,7 +324,7 @@ def run_ours(args, rank, world, local_rank):
                 times.append(dt * 1e3)
         e2e = {"value": round(sum(times) / len(times), 3), "unit": "ms",
                "h2d_bytes_per_step": m * n * 8, "d2h_bytes_per_step": m * n * 8 + n * n * 8,
-               "path": "orth.h bcgsi2P1s (host pointers, pinned), FP64"}
+               "path": f"orth.h {variant} (host pointers, pinned), {prec_name}"}
         del Xh_t, Rh_t
 
     # Roofline of the dominant kernel class.
@@ -316,12 +340,21 @@ def run_ours(args, rank, world, local_rank):
                 "peak_source": "live DFMA probe (orth_gb300_fp64_peak_probe); MEASURED_PEAKS.json has no FP64 figure",
                 "launch_ms": round(pc["ms"] / launches, 4)}
     else:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
-            if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-        peak = peaks.get("bf16_tflops", 1900.0)
-        achieved = pc["flops"] / (pc["ms"] * 1e-3) / 1e12 if pc["ms"] > 0 else 0.0
-        roof = {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak, "unit": "TFLOP/s",
-                "frac": round(achieved / peak, 4), "traffic": None, "kernel": dom}
+        mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        peaks = json.load(open(mp)) if os.path.exists(mp) else {}
+        peak = peaks.get("hbm_gbs", 6800.0)
+        achieved = pc["bytes"] / (pc["ms"] * 1e-3) / 1e9 if pc["ms"] > 0 else 0.0
+        kd = 7
+        tensor_tflops = pc["flops"] * kd * (kd + 1) / 2 / (pc["ms"] * 1e-3) / 1e12 if pc["ms"] > 0 else 0.0
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic_from_profiles(dom),
+                "kernel": {"gram": "gram_tc_kernel<7> + gram_reduce",
+                           "update": "bbuild + bdigit + update_tc_kernel<16,7>"}[dom],
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
+                "launch_ms": round(pc["ms"] / launches, 4),
+                "bytes_per_launch": round(pc["bytes"] / launches),
+                "tensor_tflops_bf16": round(tensor_tflops, 1),
+                "tensor_frac_of_bf16_peak": round(tensor_tflops / peaks.get("bf16_tflops", 1900.0), 4)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -347,6 +380,10 @@ def run_ours(args, rank, world, local_rank):
         "tflops_alg": round(flops_alg / (ms * 1e-3) / 1e12, 4),
         "fp64_ms": round(fp64_ms, 3) if fp64_ms is not None else (round(ms, 3) if prec == orth.FP64 else None),
         "accuracy": acc,
+        "fp64_accuracy": fp64_acc,
+        "split_fast_ms": round(fast_ms, 3) if fast_ms is not None else None,
+        "split_fast_accuracy": fast_acc,
+        "speedup_vs_fp64_gpu": round(fp64_ms / ms, 2) if fp64_ms else None,
         "gpu_launches": int(launches_per_qr * args.steps),
         "kernel_profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"]} for k, v in prof.items()},
         "roofline": roof,

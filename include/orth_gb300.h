@@ -22,8 +22,9 @@ typedef struct orth_gb300_status {
 } orth_gb300_status;
 
 /* Precision modes of the tall products (Q^T V and Q S). */
-#define ORTH_GB300_FP64 0        /* plain FP64 on the FP64 pipe */
-#define ORTH_GB300_SPLIT_BF16 1  /* split precision on the tensor cores */
+#define ORTH_GB300_FP64 0             /* plain FP64 on the FP64 pipe */
+#define ORTH_GB300_SPLIT_BF16 1       /* tensor cores, 7 BF16 digit planes (56-bit fixed point) */
+#define ORTH_GB300_SPLIT_BF16_FAST 2  /* tensor cores, 6 BF16 digit planes (48-bit fixed point) */
 
 /* Variant identifiers for orth_gb300_run_dev. */
 #define ORTH_GB300_BCGSI2P1S 0
@@ -64,6 +65,26 @@ int orth_gb300_bcgsi2P1s_dev_noalloc(int m, int n, int s, double *dX, long long 
                                      double *dR, int ldR, void *stream,
                                      orth_gb300_status *status);
 
+/*
+ * Precision used by the five orth.h entry points (default ORTH_GB300_FP64, the
+ * reference's arithmetic; the environment variable ORTH_GB300_PRECISION =
+ * fp64 | split | split_fast sets it at first use). Shapes the split modes do not
+ * handle (s > 32) return 4. Returns 0, or 4 for an unknown mode.
+ */
+int orth_gb300_set_host_precision(int precision);
+
+/* 1 if the split-precision mode handles (m, n, s) (s <= 32), else 0. */
+int orth_gb300_split_supported(int m, int n, int s);
+
+/*
+ * One "synchronization" on its own: C (na x nb, ldc) = X[:, 0:na]^T X[:, b0:b0+nb]
+ * for device X (m rows, ldX), in FP64 or split precision, deterministic. The
+ * reference computes it as dgemm('T','N') followed by MPI_Allreduce (for example
+ * SRC/orth.c:182-188). Waits for the stream. Return codes as orth_gb300_run_dev.
+ */
+int orth_gb300_gram_dev(int m, int na, int b0, int nb, const double *dX, long long ldX,
+                        double *dC, int ldc, int precision, void *stream);
+
 /* Status of the last run through the orth.h entry points on this thread. */
 void orth_gb300_last_status(orth_gb300_status *status);
 
@@ -76,12 +97,15 @@ long long orth_gb300_last_launch_count(void);
 /*
  * Per-kernel-class timing. orth_gb300_profile(1) resets the accumulators and
  * records a CUDA event pair on the launching stream around every kernel group
- * of later runs; orth_gb300_profile_read waits for them and returns, per class
- * (0 tall Gram + reduction, 1 tall update, 2 small s x s kernels, 3 TSQR), the
+ * of later runs; orth_gb300_profile_read waits for them and returns, per class, the
  * summed milliseconds, kernel launches, and algorithmic flops and bytes.
- * Arrays have 4 entries; any may be NULL. Returns 0 or a cudaError_t.
+ * Classes: 0 tall Gram + reduction, 1 tall update, 2 small s x s kernels,
+ * 3 TSQR, 4 digit slicing (split modes). Arrays have
+ * orth_gb300_profile_classes() entries; any may be NULL. Returns 0 or a
+ * cudaError_t.
  */
 void orth_gb300_profile(int on);
+int orth_gb300_profile_classes(void);
 int orth_gb300_profile_read(double *ms, long long *launches, double *flops, double *bytes);
 
 /* Measure the FP64 pipe's throughput (TFLOP/s) with a DFMA loop; 0 or a cudaError_t. */

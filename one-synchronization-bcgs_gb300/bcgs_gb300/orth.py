@@ -17,7 +17,8 @@ from . import build as _build
 VARIANTS = ("bcgsi2P1s", "bcgsi21s", "bcgspipi2", "bcgsi2", "bcgsi2P2s")
 VARIANT_ID = {name: i for i, name in enumerate(VARIANTS)}
 FP64 = 0
-SPLIT_BF16 = 1
+SPLIT_BF16 = 1          # 7 BF16 digit planes (56-bit fixed point)
+SPLIT_BF16_FAST = 2     # 6 BF16 digit planes (48-bit fixed point)
 
 
 class Status(ctypes.Structure):
@@ -74,6 +75,14 @@ def load(path: str | None = None):
         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong,
         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(Status)]
     lib.orth_gb300_bcgsi2P1s_dev_noalloc.restype = ctypes.c_int
+    lib.orth_gb300_set_host_precision.argtypes = [ctypes.c_int]
+    lib.orth_gb300_set_host_precision.restype = ctypes.c_int
+    lib.orth_gb300_split_supported.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.orth_gb300_split_supported.restype = ctypes.c_int
+    lib.orth_gb300_gram_dev.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    lib.orth_gb300_gram_dev.restype = ctypes.c_int
     lib.orth_gb300_reserve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.orth_gb300_reserve.restype = ctypes.c_int
     lib.orth_gb300_release.argtypes = []
@@ -150,6 +159,23 @@ def bcgsi2P1s_dev_noalloc(m: int, n: int, s: int, x_ptr: int, ldx: int, r_ptr: i
     return int(rc), st.as_dict()
 
 
+def set_host_precision(precision: int) -> int:
+    """Precision of the orth.h entry points (FP64, SPLIT_BF16, SPLIT_BF16_FAST)."""
+    return int(load().orth_gb300_set_host_precision(precision))
+
+
+def split_supported(m: int, n: int, s: int) -> bool:
+    return bool(load().orth_gb300_split_supported(m, n, s))
+
+
+def gram_dev(m: int, na: int, b0: int, nb: int, x_ptr: int, ldx: int, c_ptr: int, ldc: int,
+             precision: int = FP64, stream: int = 0) -> int:
+    """C = X[:, 0:na]^T X[:, b0:b0+nb] on device buffers (one synchronization)."""
+    return int(load().orth_gb300_gram_dev(m, na, b0, nb, ctypes.c_void_p(x_ptr), ldx,
+                                          ctypes.c_void_p(c_ptr), ldc, precision,
+                                          ctypes.c_void_p(stream)))
+
+
 def sync_count(variant: str, n: int, s: int) -> int:
     return int(load().orth_gb300_sync_count(VARIANT_ID[variant], n, s))
 
@@ -158,7 +184,7 @@ def last_launch_count() -> int:
     return int(load().orth_gb300_last_launch_count())
 
 
-PROFILE_CLASSES = ("gram", "update", "small", "tsqr")
+PROFILE_CLASSES = ("gram", "update", "small", "tsqr", "slice")
 
 
 def profile(on: bool) -> None:
@@ -168,10 +194,11 @@ def profile(on: bool) -> None:
 
 def profile_read() -> dict:
     """Per class: ms, launches, algorithmic flops and bytes since profile(True)."""
-    ms = (ctypes.c_double * 4)()
-    ln = (ctypes.c_longlong * 4)()
-    fl = (ctypes.c_double * 4)()
-    by = (ctypes.c_double * 4)()
+    k = len(PROFILE_CLASSES)
+    ms = (ctypes.c_double * k)()
+    ln = (ctypes.c_longlong * k)()
+    fl = (ctypes.c_double * k)()
+    by = (ctypes.c_double * k)()
     rc = load().orth_gb300_profile_read(ms, ln, fl, by)
     if rc != 0:
         raise RuntimeError(f"orth_gb300_profile_read failed: {rc}")

@@ -18,6 +18,10 @@ int gram_chunks_fp64(i64 m, int na, int nb, int num_sms);
 int launch_gram_fp64(const double* X, i64 ld, i64 m, int a0, int na, int b0, int nb,
                      double* out, int ldo, double* part, int nchunks, cudaStream_t st);
 
+// out (na x nb, ld ldo) = fixed-order sum of nchunks partials part[c][i + j*na].
+int launch_gram_reduce(const double* part, int nchunks, int na, int nb, double* out, int ldo,
+                       cudaStream_t st);
+
 // X[:, c0:c0+nc] = (X[:, c0:c0+nc] - X[:, q0:q0+K] S) T^{-1}; T upper (nc x nc) or null.
 int launch_update_fp64(double* X, i64 ld, i64 m, int q0, int K, int c0, int nc,
                        const double* S, int lds, const double* T, int ldt, cudaStream_t st);

@@ -7,6 +7,7 @@
 // device, so a whole QR is enqueued on one stream with no host round trip.
 #include <climits>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -20,6 +21,11 @@
 namespace bcgs {
 
 long long g_launch_count = 0;
+
+static inline bool is_split(int precision) {
+    return precision == ORTH_GB300_SPLIT_BF16 || precision == ORTH_GB300_SPLIT_BF16_FAST;
+}
+static inline int split_digits_of(int precision) { return precision == ORTH_GB300_SPLIT_BF16_FAST ? 6 : 7; }
 
 namespace {
 
@@ -61,17 +67,20 @@ std::mutex g_mu;
 
 // Optional per-kernel-class timing with CUDA events recorded on the launching
 // stream around each launch group. Classes: 0 tall Gram (incl. its reduction),
-// 1 tall update, 2 small s x s kernels, 3 TSQR.
-constexpr int kProfClasses = 4;
+// 1 tall update, 2 small s x s kernels, 3 TSQR, 4 digit slicing (split modes).
+// Algorithmic flops are FP64-equivalent (2 per multiply-add of the FP64 product);
+// algorithmic bytes are what the kernels must move: FP64 operands for the FP64
+// form, BF16 digit planes (2 bytes x digits per element) for the split forms.
+constexpr int kProfClasses = 5;
 struct ProfPending { int cls; cudaEvent_t a, b; };
 struct Prof {
     bool on = false;
     std::vector<cudaEvent_t> pool;
     std::vector<ProfPending> pending;
-    double ms[kProfClasses] = {0, 0, 0, 0};
-    long long launches[kProfClasses] = {0, 0, 0, 0};
-    double flops[kProfClasses] = {0, 0, 0, 0};
-    double bytes[kProfClasses] = {0, 0, 0, 0};
+    double ms[kProfClasses] = {0, 0, 0, 0, 0};
+    long long launches[kProfClasses] = {0, 0, 0, 0, 0};
+    double flops[kProfClasses] = {0, 0, 0, 0, 0};
+    double bytes[kProfClasses] = {0, 0, 0, 0, 0};
     cudaEvent_t get() {
         if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
         cudaEvent_t e = nullptr;
@@ -102,6 +111,20 @@ struct ProfScope {
     }
 };
 thread_local orth_gb300_status g_last_status = {0, 0, 0, 0};
+
+// Precision of the orth.h host entry points: FP64 (the reference's arithmetic)
+// unless set through orth_gb300_set_host_precision or ORTH_GB300_PRECISION
+// ("fp64", "split", "split_fast") at first use.
+int g_host_precision = -1;
+int host_precision() {
+    if (g_host_precision < 0) {
+        g_host_precision = ORTH_GB300_FP64;
+        const char* e = getenv("ORTH_GB300_PRECISION");
+        if (e && strcmp(e, "split") == 0) g_host_precision = ORTH_GB300_SPLIT_BF16;
+        if (e && strcmp(e, "split_fast") == 0) g_host_precision = ORTH_GB300_SPLIT_BF16_FAST;
+    }
+    return g_host_precision;
+}
 long long g_last_launches = 0;
 
 int init_ctx() {
@@ -163,7 +186,7 @@ int reserve(i64 m, int n, int s, int precision) {
     if (rc) return rc;
     rc = g_ctx.tsqr.ensure((size_t)tsqr_workspace_doubles(m, s) * sizeof(double));
     if (rc) return rc;
-    if (precision == ORTH_GB300_SPLIT_BF16) {
+    if (is_split(precision)) {
         rc = g_ctx.split.ensure((size_t)split_workspace_bytes(m, n, s, g_ctx.num_sms));
         if (rc) return rc;
     }
@@ -189,8 +212,14 @@ struct Engine {
     // C (na x nb, ld na) = X[:, 0:na]^T X[:, b0:b0+nb]: one synchronization.
     void gram(int na, int b0, int nb, double* C) {
         if (err || na <= 0 || nb <= 0) return;
-        ProfScope ps(0, st, 2.0 * m * na * nb, 8.0 * m * (na + nb));
-        if (precision == ORTH_GB300_SPLIT_BF16) {
+        if (is_split(precision)) {
+            ProfScope pslice(4, st, 0.0, 0.0);
+            err = split_prepare(na > b0 + nb ? na : b0 + nb, st);
+            if (err) return;
+        }
+        const double eb = is_split(precision) ? 2.0 * split_digits() : 8.0;
+        ProfScope ps(0, st, 2.0 * m * na * nb, eb * m * (na + nb));
+        if (is_split(precision)) {
             err = launch_gram_split(X, ld, m, na, b0, nb, C, na, g_ctx.split.as<char>(),
                                     g_ctx.split.bytes, g_ctx.num_sms, st);
             return;
@@ -201,9 +230,15 @@ struct Engine {
     // X[:, c0:c0+nc] = (X[:, c0:c0+nc] - X[:, 0:K] S) T^{-1}
     void update(int K, int c0, int nc, const double* S, int lds, const double* T, int ldt) {
         if (err || nc <= 0) return;
-        ProfScope ps(1, st, 2.0 * m * K * nc + (T ? (double)m * nc * nc : 0.0),
-                     8.0 * m * (K + 2.0 * nc));
-        if (precision == ORTH_GB300_SPLIT_BF16) {
+        if (is_split(precision)) {
+            ProfScope pslice(4, st, 0.0, 0.0);
+            err = split_prepare(K + nc, st);
+            if (err) return;
+        }
+        const double bytes = is_split(precision) ? 2.0 * split_digits() * m * (K + nc) + 8.0 * m * nc
+                                                 : 8.0 * m * (K + 2.0 * nc);
+        ProfScope ps(1, st, 2.0 * m * K * nc + (T ? (double)m * nc * nc : 0.0), bytes);
+        if (is_split(precision)) {
             err = launch_update_split(X, ld, m, K, c0, nc, S, lds, T, ldt, g_ctx.split.as<char>(),
                                       g_ctx.split.bytes, g_ctx.num_sms, st);
             return;
@@ -232,6 +267,7 @@ struct Engine {
         if (err) return;
         ProfScope ps(3, st, 6.0 * m * nc * nc, 8.0 * m * nc * 3.0);
         err = launch_tsqr(X, ld, m, c0, nc, Rout, ldr, g_ctx.tsqr.as<double>(), st);
+        if (is_split(precision)) split_mark_stale(c0, nc);
     }
 };
 
@@ -426,8 +462,8 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
                int precision, cudaStream_t st, orth_gb300_status* out) {
     if (!valid_args(m, n, s, ldX, ldR)) return 2;
     if (variant < 0 || variant > 4) return 2;
-    if (precision != ORTH_GB300_FP64 && precision != ORTH_GB300_SPLIT_BF16) return 4;
-    if (precision == ORTH_GB300_SPLIT_BF16 && !split_supported(m, n, s)) return 4;
+    if (precision != ORTH_GB300_FP64 && !is_split(precision)) return 4;
+    if (is_split(precision) && !split_supported(m, n, s)) return 4;
     int rc = reserve(m, n, s, precision);
     if (rc) {
         if (out) { std::memset(out, 0, sizeof(*out)); out->cuda_error = rc; }
@@ -438,6 +474,8 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
              carve_small(g_ctx.small.as<double>(), n, s), g_ctx.status.as<int>()};
     cudaError_t ce = cudaMemsetAsync(e.status, 0, kStatusWords * sizeof(int), st);
     if (ce != cudaSuccess) e.err = (int)ce;
+    if (!e.err && is_split(precision))
+        e.err = split_begin(dX, ldX, m, n, s, split_digits_of(precision), g_ctx.split.as<char>(), g_ctx.split.bytes, g_ctx.num_sms, st);
     switch (variant) {
         case ORTH_GB300_BCGSI2P1S: run_p1s(e); break;
         case ORTH_GB300_BCGSI21S: run_21s(e); break;
@@ -457,6 +495,12 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
         out->breakdown_step = h[0];
         out->breakdown_info = h[1];
         out->timeout = h[2];
+        if (!e.err && is_split(precision)) {
+            int w = 0;
+            int rc2 = split_error_word(&w, st);
+            if (rc2) e.err = rc2;
+            if (w) { out->timeout = w; e.err = (int)cudaErrorLaunchTimeout; }
+        }
         out->cuda_error = e.err;
     }
     return e.err ? 3 : 0;
@@ -542,23 +586,23 @@ extern "C" {
 
 int bcgsi2P1s(int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR, double* work,
               int lwork) {
-    return run_host(ORTH_GB300_BCGSI2P1S, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, ORTH_GB300_FP64);
+    return run_host(ORTH_GB300_BCGSI2P1S, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, host_precision());
 }
 int bcgsi21s(int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR, double* work,
              int lwork) {
-    return run_host(ORTH_GB300_BCGSI21S, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, ORTH_GB300_FP64);
+    return run_host(ORTH_GB300_BCGSI21S, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, host_precision());
 }
 int bcgspipi2(int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR, double* work,
               int lwork) {
-    return run_host(ORTH_GB300_BCGSPIPI2, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, ORTH_GB300_FP64);
+    return run_host(ORTH_GB300_BCGSPIPI2, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, host_precision());
 }
 int bcgsi2(int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR, double* work,
            int lwork) {
-    return run_host(ORTH_GB300_BCGSI2, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, ORTH_GB300_FP64);
+    return run_host(ORTH_GB300_BCGSI2, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, host_precision());
 }
 int bcgsi2P2s(int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR, double* work,
               int lwork) {
-    return run_host(ORTH_GB300_BCGSI2P2S, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, ORTH_GB300_FP64);
+    return run_host(ORTH_GB300_BCGSI2P2S, m, n, s, Xsub, ldXsub, R, ldR, work, lwork, host_precision());
 }
 
 int orth_gb300_run_dev(int variant, int m, int n, int s, double* dX, long long ldX, double* dR,
@@ -569,6 +613,46 @@ int orth_gb300_run_dev(int variant, int m, int n, int s, double* dX, long long l
 
 void orth_gb300_last_status(orth_gb300_status* status) {
     if (status) *status = g_last_status;
+}
+
+int orth_gb300_set_host_precision(int precision) {
+    if (precision != ORTH_GB300_FP64 && !is_split(precision)) return 4;
+    std::lock_guard<std::mutex> lock(g_mu);
+    g_host_precision = precision;
+    return 0;
+}
+
+int orth_gb300_split_supported(int m, int n, int s) { return split_supported(m, n, s) ? 1 : 0; }
+
+int orth_gb300_gram_dev(int m, int na, int b0, int nb, const double* dX, long long ldX, double* dC,
+                        int ldc, int precision, void* stream) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    const int n = na > b0 + nb ? na : b0 + nb;
+    if (m < 1 || na < 1 || nb < 1 || b0 < 0 || ldX < m || ldc < na || !dX || !dC) return 2;
+    if (precision != ORTH_GB300_FP64 && !is_split(precision)) return 4;
+    const int s = (nb + 1) / 2 > 0 ? (nb + 1) / 2 : 1;
+    if (is_split(precision) && (nb > 64 || !split_supported(m, n, s < 1 ? 1 : s))) return 4;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = init_ctx();
+    if (rc) return 3;
+    if (precision == ORTH_GB300_FP64) {
+        if (g_ctx.part.ensure((size_t)part_doubles(m, n, s, g_ctx.num_sms) * sizeof(double))) return 3;
+        const int chunks = gram_chunks_fp64(m, na, nb, g_ctx.num_sms);
+        rc = launch_gram_fp64(dX, ldX, m, 0, na, b0, nb, dC, ldc, g_ctx.part.as<double>(), chunks, st);
+    } else {
+        if (g_ctx.split.ensure((size_t)split_workspace_bytes(m, n, s, g_ctx.num_sms))) return 3;
+        rc = split_begin(const_cast<double*>(dX), ldX, m, n, s, split_digits_of(precision), g_ctx.split.as<char>(), g_ctx.split.bytes,
+                         g_ctx.num_sms, st);
+        if (!rc)
+            rc = launch_gram_split(dX, ldX, m, na, b0, nb, dC, ldc, g_ctx.split.as<char>(), g_ctx.split.bytes,
+                                   g_ctx.num_sms, st);
+        if (!rc) {
+            int w = 0;
+            rc = split_error_word(&w, st);
+            if (!rc && w) rc = (int)cudaErrorLaunchTimeout;
+        }
+    }
+    return rc ? 3 : 0;
 }
 
 int orth_gb300_sync_count(int variant, int n, int s) {
@@ -595,6 +679,8 @@ void orth_gb300_profile(int on) {
     }
     g_prof.on = on != 0;
 }
+
+int orth_gb300_profile_classes(void) { return kProfClasses; }
 
 int orth_gb300_profile_read(double* ms, long long* launches, double* flops, double* bytes) {
     std::lock_guard<std::mutex> lock(g_mu);

@@ -12,7 +12,22 @@ using i64 = long long;
 bool split_supported(i64 m, int n, int s);
 // Workspace bytes the split path needs for (m, n, s).
 i64 split_workspace_bytes(i64 m, int n, int s, int num_sms);
-// Same contracts as launch_gram_fp64 / launch_update_fp64.
+// Start a split-precision run on X (m x n, ld): lays out the digit stores in the
+// workspace, encodes the TMA maps and marks every column's digits stale.
+// kd: digit planes per operand, 7 (56-bit) or 6 (48-bit).
+int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t ws_bytes, int num_sms,
+                cudaStream_t st);
+// Bring the digit planes of columns [0, c_end) up to date (slices stale columns).
+int split_prepare(int c_end, cudaStream_t st);
+// Digit planes per operand of the current run.
+int split_digits();
+// Columns [c0, c0+nc) of X were rewritten outside the split kernels.
+void split_mark_stale(int c0, int nc);
+// Reads (and waits for) the split kernels' error word: 0, or the code of a wait
+// that ran out.
+int split_error_word(int* out, cudaStream_t st);
+// Same contracts as launch_gram_fp64 / launch_update_fp64 (the update requires
+// c0 == K and nc <= 32).
 int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, double* out, int ldo,
                       char* ws, size_t ws_bytes, int num_sms, cudaStream_t st);
 int launch_update_split(double* X, i64 ld, i64 m, int K, int c0, int nc, const double* S, int lds,

@@ -1,19 +1,889 @@
-// Split-precision tall products on the tensor cores (placeholder until the
-// tcgen05 kernels land: reports the shape as unsupported).
+// Split-precision tall products on the GB300 tensor cores (tcgen05, BF16 in, FP32
+// accumulate), used by the ORTH_GB300_SPLIT_BF16 mode of every variant.
+//
+// Representation. Each FP64 column c of X is held as KD balanced base-256 digit
+// planes with a per-column power-of-two scale 2^e_c (|x| < 2^e_c):
+//     x = 2^e_c * sum_{i=1..KD} d_i * 2^{-(8i-1)},   d_i in [-128, 128],
+// i.e. 8*KD bits of fixed point (KD = 7: 56 bits, KD = 6: 48 bits). Every digit is an integer of
+// at most 8 significant bits, so it is exact in BF16, and a digit product is an
+// integer below 2^14, exact in the FP32 accumulator. Products of equal weight
+// 2^{2-8(i+j)} are summed in the same TMEM columns: A-plane i is multiplied with the
+// concatenation [B_1 .. B_{KD+1-i}] (N = NB*(KD+1-i)) into TMEM column block i-1,
+// so block g-2 accumulates every product with i + j = g (products with i + j > KD+1
+// are below 2^{-8 KD} and dropped). Groups g = 2..7 are kept exact by emptying the
+// accumulator every 256 summation steps into two 64-bit integers; group g = 8
+// (weight 2^-48 relative) is summed in FP32.
+//
+// Two digit stores serve the two product shapes, both K-major for the tensor core:
+//   column store [plane][column][row]  (rows contiguous): A and B of the tall Gram
+//                                       X[:, 0:na]^T X[:, b0:b0+nb]  (sum over rows)
+//   row store    [plane][row][column]  (columns contiguous): A of the update
+//                                       [Q | X_k] * B  (sum over columns)
+// The update (X_k - Q S) T^{-1} is evaluated as one product
+//     [Q | X_k] * [-S T^{-1} ; T^{-1}]
+// with the column scales 2^{e_c} folded into the rows of the small right-hand
+// factor, so the triangular scaling also runs on the tensor cores.
+//
+// Kernels are persistent and warp-specialized (warp 0: TMA producer, warp 1: MMA
+// issuer + TMEM owner, warps 2-5: epilogue), with an A-tile ring of 16 KB slots, a
+// B ring, and two TMEM accumulators so the epilogue of one window overlaps the MMAs
+// of the next. Every wait is bounded; a timeout sets an error word and the kernel
+// winds down.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
 #include "common.cuh"
+#include "kernels.h"
 #include "split.h"
+#include "tc_common.cuh"
 
 namespace bcgs {
 
-bool split_supported(i64, int, int) { return false; }
-i64 split_workspace_bytes(i64, int, int, int) { return 0; }
-int launch_gram_split(const double*, i64, i64, int, int, int, double*, int, char*, size_t, int,
-                      cudaStream_t) {
-    return (int)cudaErrorNotSupported;
+namespace {
+
+constexpr int KD_MAX = 7;      // digit planes held by the stores
+constexpr int TILE_M = 128;    // MMA M (rows of D = TMEM lanes)
+constexpr int KCH = 64;        // K elements per chunk (one 128-byte swizzle row)
+constexpr int WIN = 4;         // chunks per accumulation window (256 summation steps)
+constexpr int RA = 8;          // A ring depth (16 KB slots)
+constexpr int RB = 2;          // B ring depth
+constexpr int A_SLOT = TILE_M * KCH * 2;   // 16 KB
+constexpr int NTHREADS = 192;  // 6 warps
+
+// ---------------------------------------------------------------------------
+// Digit extraction: x -> KD balanced base-256 digits of x * 2^{-e} (|x| < 2^e).
+// Integer arithmetic on the FP64 bit pattern only (no FP64 pipe work).
+// ---------------------------------------------------------------------------
+template <int KD>
+__device__ __forceinline__ void split_digits(double x, int e, int* d) {
+    const long long bits = __double_as_longlong(x);
+    const int E = (int)((bits >> 52) & 0x7FF);
+    long long V = 0;
+    if (E != 0 && E != 0x7FF) {
+        const unsigned long long M = (unsigned long long)(bits & 0xFFFFFFFFFFFFFLL) | (1ULL << 52);
+        int sh = E - 1075 + 8 * KD - 1 - e;  // V = M * 2^sh
+        if (sh > 9) sh = 9;
+        if (sh >= 0)
+            V = (long long)(M << sh);
+        else if (sh > -60)
+            V = (long long)((M + (1ULL << (-sh - 1))) >> (-sh));
+        if (bits < 0) V = -V;
+    }
+#pragma unroll
+    for (int i = KD - 1; i >= 1; --i) {
+        int di = (int)(V & 255);
+        if (di >= 128) di -= 256;
+        d[i] = di;
+        V = (V - di) >> 8;
+    }
+    d[0] = (int)V;
 }
-int launch_update_split(double*, i64, i64, int, int, int, const double*, int, const double*, int,
-                        char*, size_t, int, cudaStream_t) {
-    return (int)cudaErrorNotSupported;
+
+// Exponent e with max < 2^e from the bit pattern of a non-negative max.
+__device__ __forceinline__ int scale_exp(unsigned long long maxbits) {
+    const int E = (int)((maxbits >> 52) & 0x7FF);
+    return E == 0 ? 0 : E - 1022;
+}
+
+__device__ __forceinline__ unsigned short bf16_bits_of_int(int d) {
+    return __bfloat16_as_ushort(__float2bfloat16_rn((float)d));
+}
+
+// Column max |x| (bit patterns of non-negative doubles order like the values).
+__global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c0,
+                              unsigned long long* __restrict__ cmax) {
+    const int c = c0 + blockIdx.y;
+    const i64 r0 = (i64)blockIdx.x * 4096;
+    const i64 r1 = min(m, r0 + 4096);
+    unsigned long long v = 0;
+    for (i64 r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        unsigned long long b = (unsigned long long)__double_as_longlong(X[r + (i64)c * ld]) & 0x7FFFFFFFFFFFFFFFULL;
+        if ((b >> 52) == 0x7FF) b = 0;  // Inf/NaN do not set the scale
+        v = v > b ? v : b;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = v > w ? v : w;
+    }
+    __shared__ unsigned long long red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = v > red[w] ? v : red[w];
+        v = v > red[0] ? v : red[0];
+        atomicMax(cmax + c, v);
+    }
+}
+
+// Slice columns [c0, c0+nc) of X into both digit stores. A CTA handles 256 rows:
+// thread t takes row t, reads its NC values (each warp load is a coalesced 256-byte
+// run of one column), computes the digits, writes its row of each row-store plane
+// with 16-byte stores, and stages the column-store planes in shared memory so they
+// leave as coalesced 16-byte stores along the rows.
+template <int NC, int KD>
+__global__ void __launch_bounds__(256)
+slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int c0, int nc,
+             const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
+             unsigned short* __restrict__ colstore, i64 ldr, i64 plane_col,
+             unsigned short* __restrict__ rowstore, i64 ldc, i64 plane_row) {
+    extern __shared__ __align__(16) unsigned short sdig[];   // [KD][NC][256]
+    const int t = threadIdx.x;
+    const i64 r0 = (i64)blockIdx.x * 256;
+    const i64 r = r0 + t;
+    if (blockIdx.x == 0 && t < nc) cexp[c0 + t] = scale_exp(cmax[c0 + t]);
+    uint32_t packed[KD][NC / 2];
+#pragma unroll
+    for (int j = 0; j < NC; j += 2) {
+        int d0[KD], d1[KD];
+        const double x0 = (j < nc && r < m) ? X[r + (i64)(c0 + j) * ld] : 0.0;
+        const double x1 = (j + 1 < nc && r < m) ? X[r + (i64)(c0 + j + 1) * ld] : 0.0;
+        split_digits<KD>(x0, j < nc ? scale_exp(cmax[c0 + j]) : 0, d0);
+        split_digits<KD>(x1, j + 1 < nc ? scale_exp(cmax[c0 + j + 1]) : 0, d1);
+#pragma unroll
+        for (int i = 0; i < KD; ++i) {
+            const unsigned short b0 = bf16_bits_of_int(d0[i]), b1 = bf16_bits_of_int(d1[i]);
+            packed[i][j / 2] = (uint32_t)b0 | ((uint32_t)b1 << 16);
+            sdig[(i * NC + j) * 256 + t] = b0;
+            sdig[(i * NC + j + 1) * 256 + t] = b1;
+        }
+    }
+    // Row store: this row's nc digits of each plane.
+    if (r < m) {
+        const bool vec = (nc == NC) && ((c0 & 7) == 0) && ((ldc & 7) == 0);
+#pragma unroll
+        for (int i = 0; i < KD; ++i) {
+            unsigned short* dst = rowstore + (i64)i * plane_row + r * ldc + c0;
+            if (vec) {
+                uint4* d4 = reinterpret_cast<uint4*>(dst);
+#pragma unroll
+                for (int q = 0; q < NC / 8; ++q)
+                    d4[q] = make_uint4(packed[i][4 * q], packed[i][4 * q + 1], packed[i][4 * q + 2],
+                                       packed[i][4 * q + 3]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < NC; ++j)
+                    if (j < nc) dst[j] = (unsigned short)((packed[i][j / 2] >> (16 * (j & 1))) & 0xFFFFu);
+            }
+        }
+    }
+    __syncthreads();
+    // Column store: for each (plane, column), 256 rows = 32 x 16-byte pieces.
+    const bool full = (r0 + 256 <= m) && ((ldr & 7) == 0);
+    for (int e = t; e < KD * NC * 32; e += 256) {
+        const int piece = e & 31, ij = e >> 5;
+        const int i = ij / NC, j = ij % NC;
+        if (j >= nc) continue;
+        unsigned short* dst = colstore + (i64)i * plane_col + (i64)(c0 + j) * ldr + r0 + piece * 8;
+        const unsigned short* src = sdig + (i * NC + j) * 256 + piece * 8;
+        if (full) {
+            *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(src);
+        } else {
+            for (int q = 0; q < 8; ++q)
+                if (r0 + piece * 8 + q < m) dst[q] = src[q];
+        }
+    }
+}
+
+// Right-hand factor of the update, scaled: Bp[c + j*ldb] for c < K + nc, j < nc:
+//   c <  K : -(S T^{-1})[c, j] * 2^{cexp[c]}      (or -S[c, j] * 2^{cexp[c]} if T is null)
+//   c >= K :  T^{-1}[c-K, j]   * 2^{cexp[c]}      (or the identity)
+// and the per-column max |Bp| into bmax (bit patterns).
+__global__ void __launch_bounds__(256)
+bbuild_kernel(const double* __restrict__ S, int lds, const double* __restrict__ T, int ldt, int K, int nc,
+              const int* __restrict__ cexp, double* __restrict__ Bp, int ldb,
+              unsigned long long* __restrict__ bmax) {
+    __shared__ double ti[32][33];
+    const int tid = threadIdx.x;
+    // T^{-1} (upper, nc x nc): column j solves T y = e_j by back substitution.
+    if (T != nullptr) {
+        if (tid < nc) {
+            const int j = tid;
+            for (int i = nc - 1; i >= 0; --i) {
+                double v = (i == j) ? 1.0 : 0.0;
+                for (int l = i + 1; l <= j; ++l) v -= T[i + (i64)l * ldt] * ti[l][j];
+                ti[i][j] = (i <= j) ? v / T[i + (i64)i * ldt] : 0.0;
+            }
+        }
+    } else {
+        for (int e = tid; e < 32 * 32; e += blockDim.x) ti[e / 32][e % 32] = (e / 32 == e % 32) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    const int c = blockIdx.x * 64 + (tid & 63);
+    for (int j = tid >> 6; j < nc; j += 4) {
+        double v = 0.0;
+        if (c < K) {
+            if (T != nullptr) {
+                for (int l = 0; l <= j; ++l) v -= S[c + (i64)l * lds] * ti[l][j];
+            } else {
+                v = -S[c + (i64)j * lds];
+            }
+        } else if (c < K + nc) {
+            v = ti[c - K][j];
+        }
+        if (c < K + nc) {
+            v = ldexp(v, cexp[c]);
+            Bp[c + (i64)j * ldb] = v;
+            unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
+            if ((b >> 52) == 0x7FF) b = 0;
+            atomicMax(bmax + j, b);
+        }
+    }
+}
+
+// Digits of the right-hand factor: bdig[plane][j][c] (K-major), zero padded to
+// (NB rows, Kpad columns); fexp[j] = its column scale exponent.
+template <int KD>
+__global__ void __launch_bounds__(256)
+bdigit_kernel(const double* __restrict__ Bp, int ldb, int K, int nc, int NB, int Kpad,
+              const unsigned long long* __restrict__ bmax, int* __restrict__ fexp,
+              unsigned short* __restrict__ bdig) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x == 0 && threadIdx.x < NB) fexp[threadIdx.x] = threadIdx.x < nc ? scale_exp(bmax[threadIdx.x]) : 0;
+    if (c >= Kpad) return;
+    for (int j = 0; j < NB; ++j) {
+        int d[KD];
+        if (c < K + nc && j < nc) {
+            split_digits<KD>(Bp[c + (i64)j * ldb], scale_exp(bmax[j]), d);
+        } else {
+#pragma unroll
+            for (int i = 0; i < KD; ++i) d[i] = 0;
+        }
+#pragma unroll
+        for (int i = 0; i < KD; ++i) bdig[((i64)i * NB + j) * Kpad + c] = bf16_bits_of_int(d[i]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Shared mainloop pieces.
+// ---------------------------------------------------------------------------
+struct Ring {
+    int slot = 0;
+    uint32_t phase = 0;
+    __device__ __forceinline__ void advance(int R) {
+        if (++slot == R) { slot = 0; phase ^= 1u; }
+    }
+};
+
+template <int NB, int KD>
+struct SmemLayout {
+    static constexpr int B_SLOT = KD * NB * KCH * 2;
+    static constexpr int A_OFF = 0;
+    static constexpr int B_OFF = RA * A_SLOT;
+    static constexpr int BAR_OFF = B_OFF + RB * B_SLOT;
+    static constexpr int BYTES = BAR_OFF + 256 + 1024;  // barriers + alignment slack
+    static constexpr int TMEM_COLS_PER_BUF = NB * KD;
+    static constexpr int TMEM_ALLOC = (2 * TMEM_COLS_PER_BUF) <= 128 ? 128 : ((2 * TMEM_COLS_PER_BUF) <= 256 ? 256 : 512);
+};
+
+struct Bars {
+    uint64_t a_full[RA], a_empty[RA], b_full[RB], b_empty[RB], t_full[2], t_empty[2], drain;
+};
+
+// Per-window epilogue accumulation of the TMEM groups: groups 0-2 (weights 1,
+// 2^-8, 2^-16) into the exact 64-bit integer hi, groups 3-5 into the exact 64-bit
+// integer mid (weight 2^-24 relative to hi's unit), and groups >= 6 (weight <=
+// 2^-48) into FP32. Each TMEM value is an integer below 2^24.6 (at most 3 products
+// of |digit| <= 2^7 per summation step, 256 steps per window).
+template <int NB, int KD>
+__device__ __forceinline__ void accumulate_window(uint32_t taddr, long long* hi, long long* mid, float* lo) {
+#pragma unroll
+    for (int g = 0; g < KD; ++g) {
+#pragma unroll
+        for (int h = 0; h < NB / 16; ++h) {
+            float v[16];
+            tc::tmem_ld16(taddr + (uint32_t)(g * NB + h * 16), v);
+            if (g < 3) {
+                const int sh = 8 * (2 - g);
+#pragma unroll
+                for (int q = 0; q < 16; ++q) hi[h * 16 + q] += (long long)__float2int_rn(v[q]) << sh;
+            } else if (g < 6) {
+                const int sh = 8 * (5 - g);
+#pragma unroll
+                for (int q = 0; q < 16; ++q) mid[h * 16 + q] += (long long)__float2int_rn(v[q]) << sh;
+            } else {
+                const float w = __int_as_float((127 - 8 * (g - 6)) << 23);  // 2^{-8(g-6)}
+#pragma unroll
+                for (int q = 0; q < 16; ++q) lo[h * 16 + q] = fmaf(v[q], w, lo[h * 16 + q]);
+            }
+        }
+    }
+}
+
+// value * 2^{16} of one output: D_0 + D_1 2^-8 + ... in units of the group-0 weight.
+__device__ __forceinline__ double assemble(long long hi, long long mid, float lo) {
+    return (double)hi + (double)mid * 5.9604644775390625e-08 + (double)lo * 2.3283064365386963e-10;
+}
+
+// Producer: for each chunk, B planes then KD A planes (TMA).
+template <int NB, int KD, class CoordFn>
+__device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapA, const CUtensorMap* mapB, uint8_t* sA,
+                                              uint8_t* sB, Bars* bars, Ring& ra, Ring& rb, CoordFn coords,
+                                              int item, int ch, volatile int* abort, int* err) {
+    constexpr int B_SLOT = SmemLayout<NB, KD>::B_SLOT;
+    int ax, ay, bx, by;
+    coords(item, ch, ax, ay, bx, by);
+    if (!tc::mbar_wait(&bars->b_empty[rb.slot], rb.phase ^ 1u, abort, err, 11)) return false;
+    tc::mbar_expect_tx(&bars->b_full[rb.slot], (uint32_t)B_SLOT);
+#pragma unroll
+    for (int j = 0; j < KD; ++j)
+        tc::tma_load_3d(sB + rb.slot * B_SLOT + j * NB * KCH * 2, mapB, &bars->b_full[rb.slot], bx, by, j);
+    rb.advance(RB);
+#pragma unroll
+    for (int i = 0; i < KD; ++i) {
+        if (!tc::mbar_wait(&bars->a_empty[ra.slot], ra.phase ^ 1u, abort, err, 12)) return false;
+        tc::mbar_expect_tx(&bars->a_full[ra.slot], (uint32_t)A_SLOT);
+        tc::tma_load_3d(sA + ra.slot * A_SLOT, mapA, &bars->a_full[ra.slot], ax, ay, i);
+        ra.advance(RA);
+    }
+    return true;
+}
+
+// MMA issuer for one chunk into TMEM buffer `dcol` (column offset).
+template <int NB, int KD>
+__device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uint8_t* sA, uint8_t* sB,
+                                          Bars* bars, Ring& ra, Ring& rb, bool first_in_window,
+                                          volatile int* abort, int* err) {
+    constexpr int B_SLOT = SmemLayout<NB, KD>::B_SLOT;
+    if (!tc::mbar_wait(&bars->b_full[rb.slot], rb.phase, abort, err, 21)) return false;
+    const uint32_t b_addr = tc::smem_u32(sB + rb.slot * B_SLOT);
+#pragma unroll
+    for (int i = 0; i < KD; ++i) {
+        if (!tc::mbar_wait(&bars->a_full[ra.slot], ra.phase, abort, err, 22)) return false;
+        tc::tc_fence_after();
+        const uint32_t a_addr = tc::smem_u32(sA + ra.slot * A_SLOT);
+        const uint32_t idesc = tc::idesc_bf16_f32(TILE_M, NB * (KD - i));
+#pragma unroll
+        for (int k = 0; k < KCH / 16; ++k) {
+            const uint64_t da = tc::sw128_desc(a_addr + k * 32);
+            const uint64_t db = tc::sw128_desc(b_addr + k * 32);
+            const uint32_t acc = (first_in_window && i == 0 && k == 0) ? 0u : 1u;
+            tc::mma_bf16(tmem_base + dcol + (uint32_t)(i * NB), da, db, idesc, acc);
+        }
+        tc::mma_commit(&bars->a_empty[ra.slot]);
+        ra.advance(RA);
+    }
+    tc::mma_commit(&bars->b_empty[rb.slot]);
+    rb.advance(RB);
+    return true;
+}
+
+template <int NB, int KD>
+__device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint8_t*& sB, uint32_t* tmem_slot) {
+    using L = SmemLayout<NB, KD>;
+    uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    sA = base + L::A_OFF;
+    sB = base + L::B_OFF;
+    Bars* bars = reinterpret_cast<Bars*>(base + L::BAR_OFF);
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < RA; ++i) { tc::mbar_init(&bars->a_full[i], 1); tc::mbar_init(&bars->a_empty[i], 1); }
+        for (int i = 0; i < RB; ++i) { tc::mbar_init(&bars->b_full[i], 1); tc::mbar_init(&bars->b_empty[i], 1); }
+        for (int i = 0; i < 2; ++i) { tc::mbar_init(&bars->t_full[i], 1); tc::mbar_init(&bars->t_empty[i], 128); }
+        tc::mbar_init(&bars->drain, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 1) tc::tmem_alloc(tmem_slot, (uint32_t)L::TMEM_ALLOC);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    return bars;
+}
+
+// ---------------------------------------------------------------------------
+// Tall Gram: part[rc][c + j*na] = sum over rows of this CTA's range of
+// X[r, c] X[r, b0 + j] for c in the M-block, j in the N-group.
+// ---------------------------------------------------------------------------
+struct GramParams {
+    int na, nb, b0;
+    i64 m;
+    int numMB, numNG, rc;
+    i64 rows_per;   // multiple of WIN*KCH
+    const int* cexp;
+    double* part;
+    int* err;
+};
+
+template <int KD>
+__global__ void __launch_bounds__(NTHREADS, 1)
+gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GramParams p) {
+    constexpr int NB = 32;
+    using L = SmemLayout<NB, KD>;
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int abort_flag;
+    uint8_t *sA, *sB;
+    if (threadIdx.x == 0) abort_flag = 0;
+    Bars* bars = setup_cta<NB, KD>(smem_raw, sA, sB, &tmem_slot);
+    const uint32_t tmem = tmem_slot;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    const int item = blockIdx.x;
+    const int mb = item % p.numMB;
+    const int ng = (item / p.numMB) % p.numNG;
+    const int rcI = item / (p.numMB * p.numNG);
+    const i64 r0 = (i64)rcI * p.rows_per;
+    const i64 r1 = min(p.m, r0 + p.rows_per);
+    const int nchunks = r1 > r0 ? (int)ceil_div(r1 - r0, KCH) : 0;
+    const int nwin = (nchunks + WIN - 1) / WIN;
+
+    auto coords = [&](int, int ch, int& ax, int& ay, int& bx, int& by) {
+        ax = (int)(r0 + (i64)ch * KCH);
+        ay = mb * TILE_M;
+        bx = ax;
+        by = p.b0 + ng * NB;
+    };
+
+    if (warp == 0) {
+        if (lane == 0) {
+            Ring ra, rb;
+            for (int ch = 0; ch < nchunks; ++ch)
+                if (!produce_chunk<NB, KD>(&mapA, &mapB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag, p.err)) break;
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            Ring ra, rb;
+            bool ok = true;
+            for (int w = 0; w < nwin && ok; ++w) {
+                const int buf = w & 1;
+                const uint32_t tph = (uint32_t)((w >> 1) & 1);
+                if (!tc::mbar_wait(&bars->t_empty[buf], tph ^ 1u, &abort_flag, p.err, 31)) break;
+                tc::tc_fence_after();
+                const int c_end = min(nchunks, (w + 1) * WIN);
+                for (int ch = w * WIN; ch < c_end && ok; ++ch)
+                    ok = mma_chunk<NB, KD>(tmem, (uint32_t)(buf * L::TMEM_COLS_PER_BUF), sA, sB, bars, ra, rb,
+                                       ch == w * WIN, &abort_flag, p.err);
+                if (ok) tc::mma_commit(&bars->t_full[buf]);
+            }
+            tc::mma_commit(&bars->drain);
+        }
+    } else {
+        // Epilogue: thread owns TMEM lane (32*(warp%4) + lane) = A column.
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;
+        long long hi[NB], mid[NB];
+        float lo[NB];
+#pragma unroll
+        for (int j = 0; j < NB; ++j) { hi[j] = 0; mid[j] = 0; lo[j] = 0.f; }
+        bool ok = true;
+        for (int w = 0; w < nwin; ++w) {
+            const int buf = w & 1;
+            const uint32_t tph = (uint32_t)((w >> 1) & 1);
+            if (!tc::mbar_wait(&bars->t_full[buf], tph, &abort_flag, p.err, 41)) { ok = false; break; }
+            tc::tc_fence_after();
+            const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * L::TMEM_COLS_PER_BUF);
+            accumulate_window<NB, KD>(taddr, hi, mid, lo);
+            tc::tc_fence_before();
+            tc::mbar_arrive(&bars->t_empty[buf]);
+        }
+        if (ok && !abort_flag) {
+            const int c = mb * TILE_M + row;
+            if (c < p.na) {
+                const int ec = p.cexp[c];
+                double* out = p.part + (i64)rcI * p.na * p.nb;
+#pragma unroll
+                for (int jj = 0; jj < NB; ++jj) {
+                    const int j = ng * NB + jj;
+                    if (j < p.nb) {
+                        out[c + (i64)j * p.na] = ldexp(assemble(hi[jj], mid[jj], lo[jj]), ec + p.cexp[p.b0 + j] - 30);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        // All MMAs issued by this CTA have completed once `drain` fires.
+        if (lane == 0) tc::mbar_wait(&bars->drain, 0, &abort_flag, p.err, 51);
+        __syncwarp();
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tmem, (uint32_t)L::TMEM_ALLOC);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Update: X[r, c0 + j] = sum_c A[r, c] Bp[c, j] over c < K + nc, for 128-row
+// tiles (persistent over tiles).
+// ---------------------------------------------------------------------------
+struct UpdateParams {
+    i64 m;
+    int kin;      // K + nc (inner length)
+    int nc, c0;
+    i64 ld;
+    double* X;
+    const int* fexp;
+    int* err;
+};
+
+template <int NB, int KD>
+__global__ void __launch_bounds__(NTHREADS, 1)
+update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, UpdateParams p) {
+    using L = SmemLayout<NB, KD>;
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int abort_flag;
+    uint8_t *sA, *sB;
+    if (threadIdx.x == 0) abort_flag = 0;
+    Bars* bars = setup_cta<NB, KD>(smem_raw, sA, sB, &tmem_slot);
+    const uint32_t tmem = tmem_slot;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    const int ntiles = (int)ceil_div(p.m, TILE_M);
+    const int nchunks = (p.kin + KCH - 1) / KCH;
+    const int nwin = (nchunks + WIN - 1) / WIN;
+
+    auto coords = [&](int tile, int ch, int& ax, int& ay, int& bx, int& by) {
+        ax = ch * KCH;
+        ay = tile * TILE_M;
+        bx = ch * KCH;
+        by = 0;
+    };
+
+    if (warp == 0) {
+        if (lane == 0) {
+            Ring ra, rb;
+            bool ok = true;
+            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x)
+                for (int ch = 0; ch < nchunks && ok; ++ch)
+                    ok = produce_chunk<NB, KD>(&mapA, &mapB, sA, sB, bars, ra, rb, coords, tile, ch, &abort_flag, p.err);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            Ring ra, rb;
+            bool ok = true;
+            int wc = 0;  // window counter across tiles
+            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                for (int w = 0; w < nwin && ok; ++w, ++wc) {
+                    const int buf = wc & 1;
+                    const uint32_t tph = (uint32_t)((wc >> 1) & 1);
+                    if (!tc::mbar_wait(&bars->t_empty[buf], tph ^ 1u, &abort_flag, p.err, 32)) { ok = false; break; }
+                    tc::tc_fence_after();
+                    const int c_end = min(nchunks, (w + 1) * WIN);
+                    for (int ch = w * WIN; ch < c_end && ok; ++ch)
+                        ok = mma_chunk<NB, KD>(tmem, (uint32_t)(buf * L::TMEM_COLS_PER_BUF), sA, sB, bars, ra, rb,
+                                           ch == w * WIN, &abort_flag, p.err);
+                    if (ok) tc::mma_commit(&bars->t_full[buf]);
+                }
+            }
+            tc::mma_commit(&bars->drain);
+        }
+    } else {
+        const int quarter = warp & 3;
+        const int rloc = quarter * 32 + lane;
+        int wc = 0;
+        bool ok = true;
+        for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+            long long hi[NB], mid[NB];
+            float lo[NB];
+#pragma unroll
+            for (int j = 0; j < NB; ++j) { hi[j] = 0; mid[j] = 0; lo[j] = 0.f; }
+            for (int w = 0; w < nwin; ++w, ++wc) {
+                const int buf = wc & 1;
+                const uint32_t tph = (uint32_t)((wc >> 1) & 1);
+                if (!tc::mbar_wait(&bars->t_full[buf], tph, &abort_flag, p.err, 42)) { ok = false; break; }
+                tc::tc_fence_after();
+                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * L::TMEM_COLS_PER_BUF);
+                accumulate_window<NB, KD>(taddr, hi, mid, lo);
+                tc::tc_fence_before();
+                tc::mbar_arrive(&bars->t_empty[buf]);
+            }
+            if (!ok || abort_flag) break;
+            const i64 r = (i64)tile * TILE_M + rloc;
+            if (r < p.m) {
+                double* xr = p.X + r + (i64)p.c0 * p.ld;
+#pragma unroll
+                for (int j = 0; j < NB; ++j) {
+                    if (j < p.nc) {
+                        xr[(i64)j * p.ld] = ldexp(assemble(hi[j], mid[j], lo[j]), p.fexp[j] - 30);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        if (lane == 0) tc::mbar_wait(&bars->drain, 0, &abort_flag, p.err, 52);
+        __syncwarp();
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tmem, (uint32_t)L::TMEM_ALLOC);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side: workspace plan, tensor maps, digit freshness.
+// ---------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+// 3-D BF16 map: dims {inner, outer, planes}, strides in bytes, box {64, box_outer, 1}.
+int make_map3(CUtensorMap* map, void* base, i64 inner, i64 outer, i64 planes, i64 ld_elems,
+              i64 plane_elems, int box_outer) {
+    auto enc = encode_fn();
+    if (!enc) return (int)cudaErrorNotSupported;
+    cuuint64_t dims[3] = {(cuuint64_t)inner, (cuuint64_t)outer, (cuuint64_t)planes};
+    cuuint64_t strides[2] = {(cuuint64_t)ld_elems * 2, (cuuint64_t)plane_elems * 2};
+    cuuint32_t box[3] = {(cuuint32_t)KCH, (cuuint32_t)box_outer, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? 0 : (int)cudaErrorInvalidValue;
+}
+
+i64 round_up(i64 a, i64 b) { return (a + b - 1) / b * b; }
+
+struct Plan {
+    // geometry
+    double* X = nullptr;
+    i64 ld = 0, m = 0;
+    int n = 0, num_sms = kNumSMsDefault;
+    i64 ldr = 0, ldc = 0, plane_col = 0, plane_row = 0, kpad = 0;
+    // device buffers (carved from the workspace)
+    unsigned short *colstore = nullptr, *rowstore = nullptr, *bdig = nullptr;
+    int *cexp = nullptr, *fexp = nullptr, *err = nullptr;
+    unsigned long long *cmax = nullptr, *bmax = nullptr;
+    double *bfull = nullptr, *part = nullptr;
+    i64 part_doubles = 0;
+    // maps
+    CUtensorMap map_col_a, map_col_b, map_row_a, map_bdig16, map_bdig32;
+    int kd = 7;
+    std::vector<char> fresh;
+    const void* zeroed_base = nullptr;
+    size_t zeroed_bytes = 0;
+};
+Plan g_plan;
+
+struct Carve {
+    char* p;
+    size_t off = 0;
+    template <class T>
+    T* take(i64 count) {
+        off = (off + 1023) & ~(size_t)1023;
+        T* r = reinterpret_cast<T*>(p + off);
+        off += (size_t)count * sizeof(T);
+        return r;
+    }
+};
+
+i64 gram_part_doubles(i64 m, int n, int s, int num_sms) {
+    i64 best = 0;
+    for (int na = 1; na <= n; na += 1) {
+        const int nb = 2 * s;
+        const i64 mbn = ceil_div(na, TILE_M) * ceil_div(nb, 32);
+        const i64 rc = (i64)num_sms / mbn > 0 ? (i64)num_sms / mbn : 1;
+        const i64 v = rc * (i64)na * nb;
+        if (v > best) best = v;
+    }
+    (void)m;
+    return best + 1024;
+}
+
+size_t layout_bytes(i64 m, int n, int s, int num_sms, Plan* out, char* base) {
+    Carve cv{base};
+    const i64 ldr = round_up(m, 64), ldc = round_up(n, 64), kpad = round_up(n, 64);
+    const i64 plane_col = (i64)n * ldr, plane_row = m * ldc;
+    unsigned short* col = cv.take<unsigned short>(plane_col * KD_MAX);
+    unsigned short* row = cv.take<unsigned short>(plane_row * KD_MAX);
+    unsigned short* bd = cv.take<unsigned short>((i64)KD_MAX * 32 * kpad);
+    int* cexp = cv.take<int>(n + 64);
+    int* fexp = cv.take<int>(64);
+    int* err = cv.take<int>(16);
+    unsigned long long* cmax = cv.take<unsigned long long>(n + 64);
+    unsigned long long* bmax = cv.take<unsigned long long>(64);
+    double* bfull = cv.take<double>(kpad * 32);
+    const i64 pd = gram_part_doubles(m, n, s, num_sms);
+    double* part = cv.take<double>(pd);
+    if (out) {
+        out->ldr = ldr; out->ldc = ldc; out->kpad = kpad;
+        out->plane_col = plane_col; out->plane_row = plane_row;
+        out->colstore = col; out->rowstore = row; out->bdig = bd;
+        out->cexp = cexp; out->fexp = fexp; out->err = err;
+        out->cmax = cmax; out->bmax = bmax; out->bfull = bfull; out->part = part;
+        out->part_doubles = pd;
+    }
+    return cv.off + 1024;
+}
+
+int ensure_fresh(int c_begin, int c_end, cudaStream_t st) {
+    Plan& P = g_plan;
+    int c = c_begin;
+    while (c < c_end) {
+        if (P.fresh[c]) { ++c; continue; }
+        int e = c;
+        while (e < c_end && !P.fresh[e] && e - c < 32) ++e;
+        const int nc = e - c;
+        cudaError_t ce = cudaMemsetAsync(P.cmax + c, 0, (size_t)nc * sizeof(unsigned long long), st);
+        if (ce != cudaSuccess) return (int)ce;
+        dim3 g1((unsigned)ceil_div(P.m, 4096), (unsigned)nc);
+        colmax_kernel<<<g1, 256, 0, st>>>(P.X, P.ld, P.m, c, P.cmax);
+        const unsigned blocks = (unsigned)ceil_div(P.m, 256);
+#define BCGS_SLICE(NCT, KDT)                                                                         \
+    slice_kernel<NCT, KDT><<<blocks, 256, (size_t)KDT * NCT * 256 * 2, st>>>(                             \
+        P.X, P.ld, P.m, c, nc, P.cmax, P.cexp, P.colstore, P.ldr, P.plane_col, P.rowstore, P.ldc, P.plane_row)
+        if (nc <= 16) {
+            if (P.kd == 6) BCGS_SLICE(16, 6); else BCGS_SLICE(16, 7);
+        } else {
+            if (P.kd == 6) BCGS_SLICE(32, 6); else BCGS_SLICE(32, 7);
+        }
+#undef BCGS_SLICE
+        g_launch_count += 2;
+        for (int k = c; k < e; ++k) P.fresh[k] = 1;
+        c = e;
+    }
+    return (int)cudaGetLastError();
+}
+
+template <class K>
+int set_smem(K kernel, int bytes) {
+    return (int)cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+}  // namespace
+
+bool split_supported(i64 m, int n, int s) { return s >= 1 && s <= 32 && n >= 2 * s && m >= TILE_M; }
+
+i64 split_workspace_bytes(i64 m, int n, int s, int num_sms) {
+    return (i64)layout_bytes(m, n, s, num_sms, nullptr, nullptr);
+}
+
+int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t ws_bytes, int num_sms,
+                cudaStream_t st) {
+    Plan& P = g_plan;
+    if (kd != 6 && kd != 7) return (int)cudaErrorInvalidValue;
+    P.kd = kd;
+    const size_t need = layout_bytes(m, n, s, num_sms, &P, ws);
+    if (need > ws_bytes) return (int)cudaErrorInvalidValue;
+    P.X = X; P.ld = ld; P.m = m; P.n = n; P.num_sms = num_sms;
+    P.fresh.assign((size_t)n, 0);
+    // The row store must hold finite values everywhere: the last K chunk of an
+    // update reads columns past K + nc (multiplied by zero rows of the factor).
+    if (P.zeroed_base != (const void*)P.rowstore || P.zeroed_bytes < (size_t)(P.plane_row * KD_MAX * 2)) {
+        cudaError_t ce = cudaMemsetAsync(P.rowstore, 0, (size_t)P.plane_row * KD_MAX * 2, st);
+        if (ce != cudaSuccess) return (int)ce;
+        P.zeroed_base = P.rowstore;
+        P.zeroed_bytes = (size_t)P.plane_row * KD_MAX * 2;
+    }
+    cudaError_t ce = cudaMemsetAsync(P.err, 0, sizeof(int), st);
+    if (ce != cudaSuccess) return (int)ce;
+    int rc = make_map3(&P.map_col_a, P.colstore, m, n, KD_MAX, P.ldr, P.plane_col, TILE_M);
+    if (!rc) rc = make_map3(&P.map_col_b, P.colstore, m, n, KD_MAX, P.ldr, P.plane_col, 32);
+    if (!rc) rc = make_map3(&P.map_row_a, P.rowstore, n, m, KD_MAX, P.ldc, P.plane_row, TILE_M);
+    if (!rc) rc = make_map3(&P.map_bdig16, P.bdig, P.kpad, 16, KD_MAX, P.kpad, 16 * P.kpad, 16);
+    if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
+    if (rc) return rc;
+    static bool attrs = false;
+    if (!attrs) {
+        rc = set_smem(gram_tc_kernel<6>, SmemLayout<32, 6>::BYTES);
+        if (!rc) rc = set_smem(gram_tc_kernel<7>, SmemLayout<32, 7>::BYTES);
+        if (!rc) rc = set_smem(update_tc_kernel<16, 6>, SmemLayout<16, 6>::BYTES);
+        if (!rc) rc = set_smem(update_tc_kernel<16, 7>, SmemLayout<16, 7>::BYTES);
+        if (!rc) rc = set_smem(update_tc_kernel<32, 6>, SmemLayout<32, 6>::BYTES);
+        if (!rc) rc = set_smem(update_tc_kernel<32, 7>, SmemLayout<32, 7>::BYTES);
+        if (!rc) rc = set_smem(slice_kernel<16, 6>, 6 * 16 * 256 * 2);
+        if (!rc) rc = set_smem(slice_kernel<16, 7>, 7 * 16 * 256 * 2);
+        if (!rc) rc = set_smem(slice_kernel<32, 6>, 6 * 32 * 256 * 2);
+        if (!rc) rc = set_smem(slice_kernel<32, 7>, 7 * 32 * 256 * 2);
+        if (rc) return rc;
+        attrs = true;
+    }
+    return 0;
+}
+
+void split_mark_stale(int c0, int nc) {
+    for (int c = c0; c < c0 + nc && c < (int)g_plan.fresh.size(); ++c) g_plan.fresh[c] = 0;
+}
+
+int split_error_word(int* out, cudaStream_t st) {
+    cudaError_t ce = cudaMemcpyAsync(out, g_plan.err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    return (int)ce;
+}
+
+int split_prepare(int c_end, cudaStream_t st) { return ensure_fresh(0, c_end, st); }
+
+int split_digits() { return g_plan.kd; }
+
+int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, double* out, int ldo,
+                      char* ws, size_t ws_bytes, int num_sms, cudaStream_t st) {
+    (void)X; (void)ld; (void)ws; (void)ws_bytes;
+    Plan& P = g_plan;
+    if (na <= 0 || nb <= 0) return 0;
+    int rc = ensure_fresh(0, na > b0 + nb ? na : b0 + nb, st);
+    if (rc) return rc;
+    GramParams gp;
+    gp.na = na; gp.nb = nb; gp.b0 = b0; gp.m = m;
+    gp.numMB = (int)ceil_div(na, TILE_M);
+    gp.numNG = (int)ceil_div(nb, 32);
+    const int mbn = gp.numMB * gp.numNG;
+    gp.rc = num_sms / mbn > 0 ? num_sms / mbn : 1;
+    gp.rows_per = round_up(ceil_div(m, gp.rc), (i64)WIN * KCH);
+    gp.rc = (int)ceil_div(m, gp.rows_per);
+    gp.cexp = P.cexp;
+    gp.part = P.part;
+    gp.err = P.err;
+    if ((i64)gp.rc * na * nb > P.part_doubles) return (int)cudaErrorInvalidValue;
+    if (P.kd == 6)
+        gram_tc_kernel<6><<<(unsigned)(mbn * gp.rc), NTHREADS, SmemLayout<32, 6>::BYTES, st>>>(P.map_col_a,
+                                                                                              P.map_col_b, gp);
+    else
+        gram_tc_kernel<7><<<(unsigned)(mbn * gp.rc), NTHREADS, SmemLayout<32, 7>::BYTES, st>>>(P.map_col_a,
+                                                                                              P.map_col_b, gp);
+    g_launch_count += 1;
+    rc = (int)cudaGetLastError();
+    if (rc) return rc;
+    return launch_gram_reduce(P.part, gp.rc, na, nb, out, ldo, st);
+}
+
+int launch_update_split(double* X, i64 ld, i64 m, int K, int c0, int nc, const double* S, int lds,
+                        const double* T, int ldt, char* ws, size_t ws_bytes, int num_sms, cudaStream_t st) {
+    (void)ws; (void)ws_bytes;
+    Plan& P = g_plan;
+    if (nc <= 0) return 0;
+    if (c0 != K || nc > 32 || X != P.X) return (int)cudaErrorInvalidValue;
+    int rc = ensure_fresh(0, K + nc, st);
+    if (rc) return rc;
+    const int NB = nc <= 16 ? 16 : 32;
+    cudaError_t ce = cudaMemsetAsync(P.bmax, 0, 64 * sizeof(unsigned long long), st);
+    if (ce != cudaSuccess) return (int)ce;
+    const int kin = K + nc;
+    bbuild_kernel<<<(unsigned)ceil_div(kin, 64), 256, 0, st>>>(S, lds, T, ldt, K, nc, P.cexp, P.bfull,
+                                                                  (int)P.kpad, P.bmax);
+    if (P.kd == 6)
+        bdigit_kernel<6><<<(unsigned)ceil_div(P.kpad, 256), 256, 0, st>>>(P.bfull, (int)P.kpad, K, nc, NB,
+                                                                           (int)P.kpad, P.bmax, P.fexp, P.bdig);
+    else
+        bdigit_kernel<7><<<(unsigned)ceil_div(P.kpad, 256), 256, 0, st>>>(P.bfull, (int)P.kpad, K, nc, NB,
+                                                                           (int)P.kpad, P.bmax, P.fexp, P.bdig);
+    UpdateParams up;
+    up.m = m; up.kin = kin; up.nc = nc; up.c0 = c0; up.ld = ld; up.X = X; up.fexp = P.fexp; up.err = P.err;
+    const int ntiles = (int)ceil_div(m, TILE_M);
+    const int grid = ntiles < num_sms ? ntiles : num_sms;
+#define BCGS_UPD(NBT, KDT) \
+    update_tc_kernel<NBT, KDT><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(P.map_row_a, P.map_bdig##NBT, up)
+    if (NB == 16) {
+        if (P.kd == 6) BCGS_UPD(16, 6); else BCGS_UPD(16, 7);
+    } else {
+        if (P.kd == 6) BCGS_UPD(32, 6); else BCGS_UPD(32, 7);
+    }
+#undef BCGS_UPD
+    g_launch_count += 3;
+    for (int c = c0; c < c0 + nc; ++c) P.fresh[c] = 0;
+    return (int)cudaGetLastError();
 }
 
 }  // namespace bcgs

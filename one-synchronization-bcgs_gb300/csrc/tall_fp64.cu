@@ -132,6 +132,16 @@ int launch_gram_fp64(const double* X, i64 ld, i64 m, int a0, int na, int b0, int
     return (int)cudaGetLastError();
 }
 
+int launch_gram_reduce(const double* part, int nchunks, int na, int nb, double* out, int ldo,
+                       cudaStream_t st) {
+    const i64 total = (i64)na * nb;
+    int blocks = (int)ceil_div(total, 256);
+    if (blocks > 4 * 152) blocks = 4 * 152;
+    gram_reduce<<<blocks, 256, 0, st>>>(part, nchunks, na, nb, out, ldo);
+    g_launch_count += 1;
+    return (int)cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Update: Xc[r, 0:nc] = (Xc[r, :] - sum_c Q[r, c] S[c, :]) * T^{-1}.
 // One thread per row with NC register accumulators; S is staged through shared

@@ -1,0 +1,96 @@
+"""GPU tests of the split-precision (BF16 digit planes on tcgen05) path.
+
+The split mode replaces the FP64 tall products with 6 exact BF16 digit planes per
+operand (48-bit fixed point per column), so its products match FP64 to about
+2^-47 relative to the operand norms. Checked here through the C ABI:
+  * the tall Gram primitive against the FP64 Gram on ragged shapes;
+  * full QRs of every variant: LOO_2 <= 1e-12 and relative residual <= 1e-13
+    (the spec split-precision gate) and agreement with the FP64 path;
+  * bit-exact results run to run.
+"""
+import numpy as np
+import pytest
+
+import bcgs_port as port
+from bcgs_gb300 import inputs, orth
+from helpers import VARIANTS, sign_normalize
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(torch, X):
+    return torch.from_numpy(np.ascontiguousarray(X.T)).cuda()      # (n, m) == X column-major
+
+
+@pytest.mark.parametrize("shape", [(5000, 48, 16, 32), (33333, 200, 150, 40), (70000, 130, 100, 30),
+                                   (1000, 20, 0, 7), (256, 64, 32, 32)])
+def test_split_gram_matches_fp64(lib, shape):
+    torch = pytest.importorskip("torch")
+    m, na, b0, nb = shape
+    n = max(na, b0 + nb)
+    X = inputs.graded_host(m, n, 1e4, seed=m + na)
+    dX = _dev(torch, X)
+    Cs = torch.zeros((nb, na), dtype=torch.float64, device="cuda")   # na x nb col-major
+    Cf = torch.zeros_like(Cs)
+    st = torch.cuda.current_stream().cuda_stream
+    assert orth.gram_dev(m, na, b0, nb, dX.data_ptr(), m, Cf.data_ptr(), na, orth.FP64, st) == 0
+    assert orth.gram_dev(m, na, b0, nb, dX.data_ptr(), m, Cs.data_ptr(), na, orth.SPLIT_BF16, st) == 0
+    Cs, Cf = Cs.cpu().numpy().T, Cf.cpu().numpy().T
+    norms = np.linalg.norm(X, axis=0)
+    scale = np.outer(norms[:na], norms[b0:b0 + nb])
+    rel = np.max(np.abs(Cs - Cf) / scale)
+    # 48-bit digits scaled by the column max: error <= about 2^-48 (max/rms)^2 of
+    # the norm product; max/rms is about 4-6 for these columns.
+    assert rel < 2.0 ** -41, rel
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("kappa", [1e2, 1e6])
+@pytest.mark.parametrize("mode", ["split7", "split6"])
+def test_split_qr_accuracy(lib, variant, kappa, mode):
+    torch = pytest.importorskip("torch")
+    m, n, s = 100000, 96, 16
+    X = inputs.graded_host(m, n, kappa, seed=11)
+    st = torch.cuda.current_stream().cuda_stream
+    out = {}
+    split = orth.SPLIT_BF16 if mode == "split7" else orth.SPLIT_BF16_FAST
+    for prec in (orth.FP64, split):
+        dX = _dev(torch, X)
+        dR = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        rc, status = orth.run_dev(variant, m, n, s, dX.data_ptr(), m, dR.data_ptr(), n, prec, st)
+        assert rc == 0 and status["breakdown_step"] == 0 and status["timeout"] == 0, (rc, status)
+        out[prec] = (dX.cpu().numpy().T.copy(), dR.cpu().numpy().T.copy())
+    Q, R = out[split]
+    Qf, Rf = out[orth.FP64]
+    loo = port.loo_2(Q)
+    res = port.rel_residual(X, Q, np.triu(R))
+    loo_f = port.loo_2(Qf)
+    res_f = port.rel_residual(X, Qf, np.triu(Rf))
+    if mode == "split7":
+        # 56-bit digits: the FP64 parity rule, within 10x of the FP64 path's LOO and
+        # residual (floor 1e-15, about 10 u).
+        assert loo <= 10 * max(loo_f, 1e-15), (loo, loo_f)
+        assert res <= 10 * max(res_f, 1e-15), (res, res_f)
+    else:
+        # 48-bit digits: the spec gate LOO <= 1e-12, except where the variant
+        # itself loses orthogonality in FP64 (bcgsi21s at high kappa).
+        assert loo <= max(1e-12, 200 * loo_f), (loo, loo_f)
+        assert res <= 1e-12, res
+    Qs, Rs = sign_normalize(Q, np.triu(R))
+    Qfs, Rfs = sign_normalize(Qf, np.triu(Rf))
+    assert np.max(np.abs(Rs - Rfs)) <= 1e-10 * kappa * np.max(np.abs(Rfs))
+
+
+def test_split_bit_exact_run_to_run(lib):
+    torch = pytest.importorskip("torch")
+    m, n, s = 60000, 64, 16
+    X = inputs.graded_host(m, n, 1e5, seed=4)
+    st = torch.cuda.current_stream().cuda_stream
+    res = []
+    for _ in range(2):
+        dX = _dev(torch, X)
+        dR = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        rc, _ = orth.run_dev("bcgsi2P1s", m, n, s, dX.data_ptr(), m, dR.data_ptr(), n, orth.SPLIT_BF16, st)
+        assert rc == 0
+        res.append((dX.cpu().numpy(), dR.cpu().numpy()))
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
