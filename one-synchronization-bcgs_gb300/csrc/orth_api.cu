@@ -245,6 +245,19 @@ struct Engine {
         }
         err = launch_update_fp64(X, ld, m, 0, K, c0, nc, S, lds, T, ldt, st);
     }
+    // Split modes: Q_k and U_{k+1} of the lagged variants in one tensor-core pass.
+    void fused_update(int K, int nz, const double* G, int ldg, const double* Ty, const double* Sp,
+                      const double* Ts) {
+        if (err) return;
+        {
+            ProfScope pslice(4, st, 0.0, 0.0);
+            err = split_prepare(K + s + nz, st);
+            if (err) return;
+        }
+        const double bytes = 2.0 * split_digits() * m * (K + s + nz) + 8.0 * m * (s + nz);
+        ProfScope ps(1, st, 2.0 * m * K * (s + nz) + (double)m * (s * s + nz * nz), bytes);
+        err = launch_fused_update_split(X, ld, m, K, s, nz, G, ldg, Ty, Sp, K + s, Ts, g_ctx.num_sms, st);
+    }
     void pyth_chol(const double* Om, int ldom, const double* A, int lda, int k, int nz, double* T,
                    int step) {
         if (err) return;
@@ -317,6 +330,78 @@ void run_p1s(Engine& e) {
         e.pyth_chol(G + mScol, ldg, G, ldg, mScol, nY, w.Yd, i + 1); // :200-204
         e.update(mScol, mScol, nY, G, ldg, w.Yd, nY);                // :206-209  Q_k
         e.rblock(mScol, mScol, nY, w.Scol, mScol, G, ldg, w.Sd, w.Yd, 0);  // :211-215
+        mZ += s;
+        nZ = nZn;
+    }
+}
+
+// Split-precision form of C1/C2: the same operations in the same order, except
+// that the finalization of Q_k (after the step's single synchronization) and the
+// first pass of block k+1 run as one tensor-core pass over Q (Engine::fused_update),
+// so Q is read once per block step. pyth = true: BCGSI+P-1S (scaled first pass,
+// SRC/orth.c:152-218); false: BCGSI+A-1S (unscaled first pass, SRC/orth.c:307-363).
+void run_lagged_fused(Engine& e, bool pyth) {
+    const int s = e.s, n = e.n, s0 = s;
+    const int p = nblocks_after_first(n, s);
+    Small& w = e.w;
+    const int mode = pyth ? 0 : 1;
+    e.tsqr(0, s0, e.R, e.ldR);
+    double* W = w.G2;
+    int nZ = n - s - s0 < s ? n - s - s0 : s;
+    int na, nb;
+    double* G = w.G1;
+    if (pyth) {
+        e.gram(2 * s, s0, s, W);                                     // :111-114
+        e.pyth_chol(W + s0, 2 * s, W, 2 * s, s0, s, w.Sd, 1);        // :115-119
+        e.update(s0, s0, s, W, 2 * s, w.Sd, s);                      // :121-124
+    } else {
+        e.gram(s0, s0, s, w.S0);                                     // :275-278
+        e.update(s0, s0, s, w.S0, s0, nullptr, 0);                   // :280-281
+    }
+    na = 2 * s + (pyth ? nZ : 0);
+    nb = s + nZ;
+    e.gram(pyth ? na : 2 * s, s0, nb, G);                            // :127-133 / :284-287
+    int ldg = pyth ? na : 2 * s;
+    e.pyth_chol(G + s0, ldg, G, ldg, s0, s, w.Yd, 1);                // :134-137 / :288-291
+    if (pyth) e.rblock(s0, s0, s, W, 2 * s, G, ldg, w.Sd, w.Yd, 0);  // :144-147
+    else e.rblock(s0, s0, s, w.S0, s0, G, ldg, nullptr, w.Yd, 1);    // :298-302
+    if (p <= 1) {
+        e.update(s0, s0, s, G, ldg, w.Yd, s);                        // Q_2 alone
+        return;
+    }
+    int mZ = s0;
+    {
+        const int mScolN = mZ + s;
+        e.scol(G, ldg, mZ, nZ, w.Yd, w.Scol);                        // :155-159
+        if (pyth) e.pyth_chol(G + mScolN + (i64)s * ldg, ldg, w.Scol, mScolN, mScolN, nZ, w.Sd, 2);
+        e.fused_update(s0, nZ, G, ldg, w.Yd, w.Scol, pyth ? w.Sd : nullptr);
+    }
+    for (int i = 1; i < p; ++i) {
+        const int mScol = mZ + s;
+        int nY, nZn;
+        if (i < p - 1) {
+            nZn = n - (i + 1) * s - s0 < s ? n - (i + 1) * s - s0 : s;
+            na = mScol + s + (pyth ? nZn : 0);
+            nb = s + nZn;
+            nY = s;
+        } else {
+            nZn = nZ;
+            na = mScol + nZ;
+            nb = nZ;
+            nY = nZ;
+        }
+        e.gram(na, mScol, nb, G);                                    // the one synchronization
+        ldg = na;
+        e.pyth_chol(G + mScol, ldg, G, ldg, mScol, nY, w.Yd, i + 1);
+        e.rblock(mScol, mScol, nY, w.Scol, mScol, G, ldg, pyth ? w.Sd : nullptr, w.Yd, mode);
+        if (i < p - 1) {
+            const int mZn = mZ + s, mScolN = mZn + s;
+            e.scol(G, ldg, mZn, nZn, w.Yd, w.Scol);
+            if (pyth) e.pyth_chol(G + mScolN + (i64)s * ldg, ldg, w.Scol, mScolN, mScolN, nZn, w.Sd, i + 2);
+            e.fused_update(mScol, nZn, G, ldg, w.Yd, w.Scol, pyth ? w.Sd : nullptr);
+        } else {
+            e.update(mScol, mScol, nY, G, ldg, w.Yd, nY);            // last Q_k
+        }
         mZ += s;
         nZ = nZn;
     }
@@ -477,8 +562,12 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
     if (!e.err && is_split(precision))
         e.err = split_begin(dX, ldX, m, n, s, split_digits_of(precision), g_ctx.split.as<char>(), g_ctx.split.bytes, g_ctx.num_sms, st);
     switch (variant) {
-        case ORTH_GB300_BCGSI2P1S: run_p1s(e); break;
-        case ORTH_GB300_BCGSI21S: run_21s(e); break;
+        case ORTH_GB300_BCGSI2P1S:
+            if (is_split(precision) && s <= 16) run_lagged_fused(e, true); else run_p1s(e);
+            break;
+        case ORTH_GB300_BCGSI21S:
+            if (is_split(precision) && s <= 16) run_lagged_fused(e, false); else run_21s(e);
+            break;
         case ORTH_GB300_BCGSPIPI2: run_pipi(e); break;
         case ORTH_GB300_BCGSI2: run_bcgsi2(e); break;
         default: run_p2s(e); break;

@@ -53,14 +53,16 @@ constexpr int WIN = 4;         // chunks per accumulation window (256 summation 
 constexpr int RA = 8;          // A ring depth (16 KB slots)
 constexpr int RB = 2;          // B ring depth
 constexpr int A_SLOT = TILE_M * KCH * 2;   // 16 KB
-constexpr int NTHREADS = 192;  // 6 warps
+constexpr int NTHREADS = 320;  // 10 warps: producer, MMA, 8 epilogue
+constexpr int NEPI = 256;      // epilogue threads (two per TMEM lane)
 
 // ---------------------------------------------------------------------------
 // Digit extraction: x -> KD balanced base-256 digits of x * 2^{-e} (|x| < 2^e).
 // Integer arithmetic on the FP64 bit pattern only (no FP64 pipe work).
 // ---------------------------------------------------------------------------
 template <int KD>
-__device__ __forceinline__ void split_digits(double x, int e, int* d) {
+__device__ __forceinline__ long long fixed_point_of(double x, int e) {
+    // V = round(x * 2^{8 KD - 1 - e}) from the FP64 bit pattern (|x| < 2^e).
     const long long bits = __double_as_longlong(x);
     const int E = (int)((bits >> 52) & 0x7FF);
     long long V = 0;
@@ -74,14 +76,19 @@ __device__ __forceinline__ void split_digits(double x, int e, int* d) {
             V = (long long)((M + (1ULL << (-sh - 1))) >> (-sh));
         if (bits < 0) V = -V;
     }
+    return V;
+}
+
+// Balanced digits d_0 (most significant) .. d_{KD-1} in [-128, 128] of V. With the
+// bias 0x80 added to each of the KD-1 low bytes, byte i of V + bias is d + 128 for
+// the low digits and the remaining high part is d_0.
+template <int KD>
+__device__ __forceinline__ void split_digits(double x, int e, int* d) {
+    constexpr unsigned long long kBias = 0x8080808080808080ULL >> (8 * (8 - (KD - 1)));
+    const long long Vb = fixed_point_of<KD>(x, e) + (long long)kBias;
 #pragma unroll
-    for (int i = KD - 1; i >= 1; --i) {
-        int di = (int)(V & 255);
-        if (di >= 128) di -= 256;
-        d[i] = di;
-        V = (V - di) >> 8;
-    }
-    d[0] = (int)V;
+    for (int i = 1; i < KD; ++i) d[i] = (int)((Vb >> (8 * (KD - 1 - i))) & 255) - 128;
+    d[0] = (int)(Vb >> (8 * (KD - 1)));
 }
 
 // Exponent e with max < 2^e from the bit pattern of a non-negative max.
@@ -90,8 +97,11 @@ __device__ __forceinline__ int scale_exp(unsigned long long maxbits) {
     return E == 0 ? 0 : E - 1022;
 }
 
+// BF16 bits of a small integer |d| <= 2^8 (exact: at most 8 significant bits),
+// through the FP32 magic constant 1.5 * 2^23 instead of a conversion instruction.
 __device__ __forceinline__ unsigned short bf16_bits_of_int(int d) {
-    return __bfloat16_as_ushort(__float2bfloat16_rn((float)d));
+    const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
+    return (unsigned short)(__float_as_uint(f) >> 16);
 }
 
 // Column max |x| (bit patterns of non-negative doubles order like the values).
@@ -121,66 +131,66 @@ __global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c
     }
 }
 
-// Slice columns [c0, c0+nc) of X into both digit stores. A CTA handles 256 rows:
-// thread t takes row t, reads its NC values (each warp load is a coalesced 256-byte
-// run of one column), computes the digits, writes its row of each row-store plane
-// with 16-byte stores, and stages the column-store planes in shared memory so they
-// leave as coalesced 16-byte stores along the rows.
-template <int NC, int KD>
-__global__ void __launch_bounds__(256)
+// Slice columns [c0, c0+nc) of X into both digit stores. A CTA handles 128 rows x
+// 8 columns (grid: row tiles x column groups), one row per thread: 8 coalesced
+// column loads, the digits, one 16-byte row-store piece per plane, and the
+// column-store planes staged in shared memory so they leave as 16-byte stores
+// along the rows. Small CTAs keep many loads in flight per SM.
+template <int KD>
+__global__ void __launch_bounds__(128, 4)
 slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int c0, int nc,
              const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
              unsigned short* __restrict__ colstore, i64 ldr, i64 plane_col,
              unsigned short* __restrict__ rowstore, i64 ldc, i64 plane_row) {
-    extern __shared__ __align__(16) unsigned short sdig[];   // [KD][NC][256]
+    constexpr int CG = 16;                   // columns per CTA (one 32-byte row-store sector)
+    __shared__ __align__(16) unsigned short sdig[KD][CG][128];
     const int t = threadIdx.x;
-    const i64 r0 = (i64)blockIdx.x * 256;
+    const int g = blockIdx.y * CG;           // first column of this group (relative to c0)
+    const i64 r0 = (i64)blockIdx.x * 128;
     const i64 r = r0 + t;
-    if (blockIdx.x == 0 && t < nc) cexp[c0 + t] = scale_exp(cmax[c0 + t]);
-    uint32_t packed[KD][NC / 2];
+    if (blockIdx.x == 0 && t < CG && g + t < nc) cexp[c0 + g + t] = scale_exp(cmax[c0 + g + t]);
+    double x[CG];
 #pragma unroll
-    for (int j = 0; j < NC; j += 2) {
+    for (int j = 0; j < CG; ++j) x[j] = (g + j < nc && r < m) ? X[r + (i64)(c0 + g + j) * ld] : 0.0;
+    uint32_t packed[KD][CG / 2];
+#pragma unroll
+    for (int j = 0; j < CG; j += 2) {
         int d0[KD], d1[KD];
-        const double x0 = (j < nc && r < m) ? X[r + (i64)(c0 + j) * ld] : 0.0;
-        const double x1 = (j + 1 < nc && r < m) ? X[r + (i64)(c0 + j + 1) * ld] : 0.0;
-        split_digits<KD>(x0, j < nc ? scale_exp(cmax[c0 + j]) : 0, d0);
-        split_digits<KD>(x1, j + 1 < nc ? scale_exp(cmax[c0 + j + 1]) : 0, d1);
+        split_digits<KD>(x[j], g + j < nc ? scale_exp(cmax[c0 + g + j]) : 0, d0);
+        split_digits<KD>(x[j + 1], g + j + 1 < nc ? scale_exp(cmax[c0 + g + j + 1]) : 0, d1);
 #pragma unroll
         for (int i = 0; i < KD; ++i) {
             const unsigned short b0 = bf16_bits_of_int(d0[i]), b1 = bf16_bits_of_int(d1[i]);
             packed[i][j / 2] = (uint32_t)b0 | ((uint32_t)b1 << 16);
-            sdig[(i * NC + j) * 256 + t] = b0;
-            sdig[(i * NC + j + 1) * 256 + t] = b1;
+            sdig[i][j][t] = b0;
+            sdig[i][j + 1][t] = b1;
         }
     }
-    // Row store: this row's nc digits of each plane.
     if (r < m) {
-        const bool vec = (nc == NC) && ((c0 & 7) == 0) && ((ldc & 7) == 0);
+        const bool vec = (g + CG <= nc) && (((c0 + g) & 7) == 0) && ((ldc & 7) == 0);
 #pragma unroll
         for (int i = 0; i < KD; ++i) {
-            unsigned short* dst = rowstore + (i64)i * plane_row + r * ldc + c0;
+            unsigned short* dst = rowstore + (i64)i * plane_row + r * ldc + c0 + g;
             if (vec) {
                 uint4* d4 = reinterpret_cast<uint4*>(dst);
-#pragma unroll
-                for (int q = 0; q < NC / 8; ++q)
-                    d4[q] = make_uint4(packed[i][4 * q], packed[i][4 * q + 1], packed[i][4 * q + 2],
-                                       packed[i][4 * q + 3]);
+                d4[0] = make_uint4(packed[i][0], packed[i][1], packed[i][2], packed[i][3]);
+                d4[1] = make_uint4(packed[i][4], packed[i][5], packed[i][6], packed[i][7]);
             } else {
 #pragma unroll
-                for (int j = 0; j < NC; ++j)
-                    if (j < nc) dst[j] = (unsigned short)((packed[i][j / 2] >> (16 * (j & 1))) & 0xFFFFu);
+                for (int j = 0; j < CG; ++j)
+                    if (g + j < nc) dst[j] = (unsigned short)((packed[i][j / 2] >> (16 * (j & 1))) & 0xFFFFu);
             }
         }
     }
     __syncthreads();
-    // Column store: for each (plane, column), 256 rows = 32 x 16-byte pieces.
-    const bool full = (r0 + 256 <= m) && ((ldr & 7) == 0);
-    for (int e = t; e < KD * NC * 32; e += 256) {
-        const int piece = e & 31, ij = e >> 5;
-        const int i = ij / NC, j = ij % NC;
-        if (j >= nc) continue;
-        unsigned short* dst = colstore + (i64)i * plane_col + (i64)(c0 + j) * ldr + r0 + piece * 8;
-        const unsigned short* src = sdig + (i * NC + j) * 256 + piece * 8;
+    // Column store: per (plane, column) 128 rows = 16 pieces of 16 bytes.
+    const bool full = (r0 + 128 <= m) && ((ldr & 7) == 0);
+    for (int e = t; e < KD * CG * 16; e += 128) {
+        const int piece = e & 15, ij = e >> 4;
+        const int i = ij / CG, j = ij % CG;
+        if (g + j >= nc) continue;
+        unsigned short* dst = colstore + (i64)i * plane_col + (i64)(c0 + g + j) * ldr + r0 + piece * 8;
+        const unsigned short* src = &sdig[i][j][piece * 8];
         if (full) {
             *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(src);
         } else {
@@ -233,6 +243,87 @@ bbuild_kernel(const double* __restrict__ S, int lds, const double* __restrict__ 
             if ((b >> 52) == 0x7FF) b = 0;
             atomicMax(bmax + j, b);
         }
+    }
+}
+
+// Right-hand factor of the fused update of the lagged one-sync variants. With
+// Q = X[:, 0:K], U_k = X[:, K:K+s], X_{k+1} = X[:, K+s:K+s+nz] it produces, in one
+// product over those K + s + nz columns,
+//   Q_k     = (U_k - Q Y) Ty^{-1}                      (columns j < s)
+//   U_{k+1} = (X_{k+1} - [Q Q_k] S') Ts^{-1}           (columns s + l, l < nz)
+// by substituting Q_k into the second line: with M = Ty^{-1} S'_mid and W = Ts^{-1},
+//   rows of Q:        [-Y Ty^{-1}        | (-S'_top + Y M) W]
+//   rows of U_k:      [ Ty^{-1}          | -M W             ]
+//   rows of X_{k+1}:  [ 0                |  W               ]
+// (Y = G[0:K, 0:s], S' = [S'_top; S'_mid] of K + s rows; W = I when Ts is null, the
+// unscaled first pass of bcgsi21s). Rows are scaled by 2^cexp[c]; bmax collects
+// the column maxima.
+__global__ void __launch_bounds__(256)
+bbuild_fused_kernel(const double* __restrict__ G, int ldg, int K, int s, const double* __restrict__ Ty,
+                    int ldty, const double* __restrict__ Sp, int ldsp, const double* __restrict__ Ts,
+                    int ldts, int nz, const int* __restrict__ cexp, double* __restrict__ Bp, int ldb,
+                    unsigned long long* __restrict__ bmax) {
+    __shared__ double w1[16][17], w2[16][17], mm[16][17];
+    const int tid = threadIdx.x;
+    // Ty^{-1} and Ts^{-1} (upper), one column per thread.
+    if (tid < s) {
+        const int j = tid;
+        for (int i = s - 1; i >= 0; --i) {
+            double v = (i == j) ? 1.0 : 0.0;
+            for (int l = i + 1; l <= j; ++l) v -= Ty[i + (i64)l * ldty] * w1[l][j];
+            w1[i][j] = (i <= j) ? v / Ty[i + (i64)i * ldty] : 0.0;
+        }
+    } else if (tid >= 32 && tid < 32 + nz) {
+        const int j = tid - 32;
+        for (int i = nz - 1; i >= 0; --i) {
+            double v = (i == j) ? 1.0 : 0.0;
+            if (Ts != nullptr) {
+                for (int l = i + 1; l <= j; ++l) v -= Ts[i + (i64)l * ldts] * w2[l][j];
+                w2[i][j] = (i <= j) ? v / Ts[i + (i64)i * ldts] : 0.0;
+            } else {
+                w2[i][j] = v;
+            }
+        }
+    }
+    __syncthreads();
+    // M = Ty^{-1} S'_mid  (s x nz)
+    for (int e = tid; e < s * nz; e += blockDim.x) {
+        const int a = e % s, l = e / s;
+        double v = 0.0;
+        for (int b = a; b < s; ++b) v += w1[a][b] * Sp[(K + b) + (i64)l * ldsp];
+        mm[a][l] = v;
+    }
+    __syncthreads();
+    const int kin = K + s + nz, nout = s + nz;
+    const int c = blockIdx.x * 64 + (tid & 63);
+    if (c >= kin) return;
+    for (int j = tid >> 6; j < nout; j += 4) {
+        double v = 0.0;
+        if (j < s) {
+            if (c < K) {
+                for (int l = 0; l <= j; ++l) v -= G[c + (i64)l * ldg] * w1[l][j];
+            } else if (c < K + s) {
+                v = w1[c - K][j];
+            }
+        } else {
+            const int l = j - s;
+            if (c < K) {
+                for (int q = 0; q <= l; ++q) {
+                    double tq = -Sp[c + (i64)q * ldsp];
+                    for (int a = 0; a < s; ++a) tq += G[c + (i64)a * ldg] * mm[a][q];
+                    v += tq * w2[q][l];
+                }
+            } else if (c < K + s) {
+                for (int q = 0; q <= l; ++q) v -= mm[c - K][q] * w2[q][l];
+            } else {
+                v = w2[c - K - s][l];
+            }
+        }
+        v = ldexp(v, cexp[c]);
+        Bp[c + (i64)j * ldb] = v;
+        unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
+        if ((b >> 52) == 0x7FF) b = 0;
+        atomicMax(bmax + j, b);
     }
 }
 
@@ -291,33 +382,57 @@ struct Bars {
 // 2^-48) into FP32. Each TMEM value is an integer below 2^24.6 (at most 3 products
 // of |digit| <= 2^7 per summation step, 256 steps per window).
 template <int NB, int KD>
-__device__ __forceinline__ void accumulate_window(uint32_t taddr, long long* hi, long long* mid, float* lo) {
+__device__ __forceinline__ void accumulate_window(uint32_t taddr, int col0, long long* hi, long long* mid,
+                                                  float* lo) {
+    constexpr int NH = NB / 2;   // columns of this thread's half
 #pragma unroll
     for (int g = 0; g < KD; ++g) {
+        float v[NH];
+        if (NH == 16) tc::tmem_ld16(taddr + (uint32_t)(g * NB + col0), v);
+        else tc::tmem_ld8(taddr + (uint32_t)(g * NB + col0), v);
+        if (g < 3) {
+            const int sh = 8 * (2 - g);
 #pragma unroll
-        for (int h = 0; h < NB / 16; ++h) {
-            float v[16];
-            tc::tmem_ld16(taddr + (uint32_t)(g * NB + h * 16), v);
-            if (g < 3) {
-                const int sh = 8 * (2 - g);
+            for (int q = 0; q < NH; ++q) hi[q] += (long long)__float2int_rn(v[q]) << sh;
+        } else if (g < 6) {
+            const int sh = 8 * (5 - g);
 #pragma unroll
-                for (int q = 0; q < 16; ++q) hi[h * 16 + q] += (long long)__float2int_rn(v[q]) << sh;
-            } else if (g < 6) {
-                const int sh = 8 * (5 - g);
+            for (int q = 0; q < NH; ++q) mid[q] += (long long)__float2int_rn(v[q]) << sh;
+        } else {
+            const float w = __int_as_float((127 - 8 * (g - 6)) << 23);  // 2^{-8(g-6)}
 #pragma unroll
-                for (int q = 0; q < 16; ++q) mid[h * 16 + q] += (long long)__float2int_rn(v[q]) << sh;
-            } else {
-                const float w = __int_as_float((127 - 8 * (g - 6)) << 23);  // 2^{-8(g-6)}
-#pragma unroll
-                for (int q = 0; q < 16; ++q) lo[h * 16 + q] = fmaf(v[q], w, lo[h * 16 + q]);
-            }
+            for (int q = 0; q < NH; ++q) lo[q] = fmaf(v[q], w, lo[q]);
         }
     }
 }
 
-// value * 2^{16} of one output: D_0 + D_1 2^-8 + ... in units of the group-0 weight.
-__device__ __forceinline__ double assemble(long long hi, long long mid, float lo) {
-    return (double)hi + (double)mid * 5.9604644775390625e-08 + (double)lo * 2.3283064365386963e-10;
+// The FP64 value (hi * 2^48 + mid * 2^24 + lo * 2^16) * 2^e2, rounded to nearest,
+// built with integer operations only (the FP64 pipe of GB300 runs at 2 operations
+// per SM per clock, too slow for a per-element epilogue). With the group weights
+// hi = D0 2^16 + D1 2^8 + D2, mid = D3 2^16 + D4 2^8 + D5, lo = D6 + D7 2^-8 + ...,
+// W = 2^64 * sum_g D_g 2^{-8g}.
+__device__ __forceinline__ double assemble(long long hi, long long mid, float lo, int e2) {
+    const __int128 W = ((__int128)hi << 48) + ((__int128)mid << 24) + (__int128)__float2ll_rn(lo * 65536.0f);
+    if (W == 0) return 0.0;
+    const unsigned long long sign = W < 0 ? 0x8000000000000000ULL : 0ULL;
+    const unsigned __int128 A = W < 0 ? (unsigned __int128)(-W) : (unsigned __int128)W;
+    const unsigned long long ah = (unsigned long long)(A >> 64), al = (unsigned long long)A;
+    const int p = ah ? 127 - __clzll((long long)ah) : 63 - __clzll((long long)al);  // leading bit
+    unsigned long long mant;
+    int pe = p;
+    if (p > 52) {
+        const int sh = p - 52;
+        mant = (unsigned long long)(A >> sh);
+        const unsigned long long rbit = (unsigned long long)(A >> (sh - 1)) & 1ULL;
+        mant += rbit;
+        if (mant >> 53) { mant >>= 1; ++pe; }
+    } else {
+        mant = al << (52 - p);
+    }
+    const int E = pe + e2 + 1023;
+    if (E <= 0) return __longlong_as_double((long long)sign);
+    if (E >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ULL));
+    return __longlong_as_double((long long)(sign | ((unsigned long long)E << 52) | (mant & 0xFFFFFFFFFFFFFULL)));
 }
 
 // Producer: for each chunk, B planes then KD A planes (TMA).
@@ -384,7 +499,7 @@ __device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint
     if (threadIdx.x == 0) {
         for (int i = 0; i < RA; ++i) { tc::mbar_init(&bars->a_full[i], 1); tc::mbar_init(&bars->a_empty[i], 1); }
         for (int i = 0; i < RB; ++i) { tc::mbar_init(&bars->b_full[i], 1); tc::mbar_init(&bars->b_empty[i], 1); }
-        for (int i = 0; i < 2; ++i) { tc::mbar_init(&bars->t_full[i], 1); tc::mbar_init(&bars->t_empty[i], 128); }
+        for (int i = 0; i < 2; ++i) { tc::mbar_init(&bars->t_full[i], 1); tc::mbar_init(&bars->t_empty[i], NEPI); }
         tc::mbar_init(&bars->drain, 1);
         tc::fence_mbar_init();
     }
@@ -463,13 +578,16 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
             tc::mma_commit(&bars->drain);
         }
     } else {
-        // Epilogue: thread owns TMEM lane (32*(warp%4) + lane) = A column.
+        // Epilogue: two threads per TMEM lane (32*(warp%4) + lane) = A column, each
+        // owning half of the NB output columns.
+        constexpr int NH = NB / 2;
         const int quarter = warp & 3;
+        const int half = (warp - 2) >> 2;
         const int row = quarter * 32 + lane;
-        long long hi[NB], mid[NB];
-        float lo[NB];
+        long long hi[NH], mid[NH];
+        float lo[NH];
 #pragma unroll
-        for (int j = 0; j < NB; ++j) { hi[j] = 0; mid[j] = 0; lo[j] = 0.f; }
+        for (int j = 0; j < NH; ++j) { hi[j] = 0; mid[j] = 0; lo[j] = 0.f; }
         bool ok = true;
         for (int w = 0; w < nwin; ++w) {
             const int buf = w & 1;
@@ -477,7 +595,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
             if (!tc::mbar_wait(&bars->t_full[buf], tph, &abort_flag, p.err, 41)) { ok = false; break; }
             tc::tc_fence_after();
             const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * L::TMEM_COLS_PER_BUF);
-            accumulate_window<NB, KD>(taddr, hi, mid, lo);
+            accumulate_window<NB, KD>(taddr, half * NH, hi, mid, lo);
             tc::tc_fence_before();
             tc::mbar_arrive(&bars->t_empty[buf]);
         }
@@ -487,11 +605,9 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
                 const int ec = p.cexp[c];
                 double* out = p.part + (i64)rcI * p.na * p.nb;
 #pragma unroll
-                for (int jj = 0; jj < NB; ++jj) {
-                    const int j = ng * NB + jj;
-                    if (j < p.nb) {
-                        out[c + (i64)j * p.na] = ldexp(assemble(hi[jj], mid[jj], lo[jj]), ec + p.cexp[p.b0 + j] - 30);
-                    }
+                for (int jj = 0; jj < NH; ++jj) {
+                    const int j = ng * NB + half * NH + jj;
+                    if (j < p.nb) out[c + (i64)j * p.na] = assemble(hi[jj], mid[jj], lo[jj], ec + p.cexp[p.b0 + j] - 78);
                 }
             }
         }
@@ -517,6 +633,7 @@ struct UpdateParams {
     i64 ld;
     double* X;
     const int* fexp;
+    unsigned long long* cmax;   // column max |X[:, c0 + j]| of the written block (bit patterns)
     int* err;
 };
 
@@ -536,6 +653,9 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     const int ntiles = (int)ceil_div(p.m, TILE_M);
     const int nchunks = (p.kin + KCH - 1) / KCH;
     const int nwin = (nchunks + WIN - 1) / WIN;
+    __shared__ unsigned long long s_cmax[32];
+    if (threadIdx.x < 32) s_cmax[threadIdx.x] = 0ULL;
+    __syncthreads();
 
     auto coords = [&](int tile, int ch, int& ax, int& ay, int& bx, int& by) {
         ax = ch * KCH;
@@ -573,39 +693,51 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
             tc::mma_commit(&bars->drain);
         }
     } else {
+        constexpr int NH = NB / 2;
         const int quarter = warp & 3;
+        const int half = (warp - 2) >> 2;
         const int rloc = quarter * 32 + lane;
         int wc = 0;
         bool ok = true;
         for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-            long long hi[NB], mid[NB];
-            float lo[NB];
+            long long hi[NH], mid[NH];
+            float lo[NH];
 #pragma unroll
-            for (int j = 0; j < NB; ++j) { hi[j] = 0; mid[j] = 0; lo[j] = 0.f; }
+            for (int j = 0; j < NH; ++j) { hi[j] = 0; mid[j] = 0; lo[j] = 0.f; }
             for (int w = 0; w < nwin; ++w, ++wc) {
                 const int buf = wc & 1;
                 const uint32_t tph = (uint32_t)((wc >> 1) & 1);
                 if (!tc::mbar_wait(&bars->t_full[buf], tph, &abort_flag, p.err, 42)) { ok = false; break; }
                 tc::tc_fence_after();
                 const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * L::TMEM_COLS_PER_BUF);
-                accumulate_window<NB, KD>(taddr, hi, mid, lo);
+                accumulate_window<NB, KD>(taddr, half * NH, hi, mid, lo);
                 tc::tc_fence_before();
                 tc::mbar_arrive(&bars->t_empty[buf]);
             }
             if (!ok || abort_flag) break;
             const i64 r = (i64)tile * TILE_M + rloc;
-            if (r < p.m) {
-                double* xr = p.X + r + (i64)p.c0 * p.ld;
+            double* xr = p.X + r + (i64)p.c0 * p.ld;
 #pragma unroll
-                for (int j = 0; j < NB; ++j) {
-                    if (j < p.nc) {
-                        xr[(i64)j * p.ld] = ldexp(assemble(hi[j], mid[j], lo[j]), p.fexp[j] - 30);
-                    }
+            for (int jj = 0; jj < NH; ++jj) {
+                const int j = half * NH + jj;
+                unsigned long long a = 0ULL;
+                if (j < p.nc && r < p.m) {
+                    const double v = assemble(hi[jj], mid[jj], lo[jj], p.fexp[j] - 78);
+                    xr[(i64)j * p.ld] = v;
+                    a = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
+                    if ((a >> 52) == 0x7FF) a = 0ULL;
                 }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const unsigned long long b = __shfl_xor_sync(0xffffffffu, a, o);
+                    a = a > b ? a : b;
+                }
+                if (lane == 0 && a) atomicMax(&s_cmax[j], a);
             }
         }
     }
     __syncthreads();
+    if (threadIdx.x < p.nc && s_cmax[threadIdx.x]) atomicMax(p.cmax + p.c0 + threadIdx.x, s_cmax[threadIdx.x]);
     if (warp == 1) {
         if (lane == 0) tc::mbar_wait(&bars->drain, 0, &abort_flag, p.err, 52);
         __syncwarp();
@@ -663,6 +795,7 @@ struct Plan {
     CUtensorMap map_col_a, map_col_b, map_row_a, map_bdig16, map_bdig32;
     int kd = 7;
     std::vector<char> fresh;
+    std::vector<char> cmax_valid;   // cmax[c] already holds max |X[:, c]| (set by the update)
     const void* zeroed_base = nullptr;
     size_t zeroed_bytes = 0;
 };
@@ -725,24 +858,24 @@ int ensure_fresh(int c_begin, int c_end, cudaStream_t st) {
     while (c < c_end) {
         if (P.fresh[c]) { ++c; continue; }
         int e = c;
-        while (e < c_end && !P.fresh[e] && e - c < 32) ++e;
+        while (e < c_end && !P.fresh[e] && e - c < 32 && P.cmax_valid[e] == P.cmax_valid[c]) ++e;
         const int nc = e - c;
-        cudaError_t ce = cudaMemsetAsync(P.cmax + c, 0, (size_t)nc * sizeof(unsigned long long), st);
-        if (ce != cudaSuccess) return (int)ce;
-        dim3 g1((unsigned)ceil_div(P.m, 4096), (unsigned)nc);
-        colmax_kernel<<<g1, 256, 0, st>>>(P.X, P.ld, P.m, c, P.cmax);
-        const unsigned blocks = (unsigned)ceil_div(P.m, 256);
-#define BCGS_SLICE(NCT, KDT)                                                                         \
-    slice_kernel<NCT, KDT><<<blocks, 256, (size_t)KDT * NCT * 256 * 2, st>>>(                             \
-        P.X, P.ld, P.m, c, nc, P.cmax, P.cexp, P.colstore, P.ldr, P.plane_col, P.rowstore, P.ldc, P.plane_row)
-        if (nc <= 16) {
-            if (P.kd == 6) BCGS_SLICE(16, 6); else BCGS_SLICE(16, 7);
-        } else {
-            if (P.kd == 6) BCGS_SLICE(32, 6); else BCGS_SLICE(32, 7);
+        if (!P.cmax_valid[c]) {
+            cudaError_t ce = cudaMemsetAsync(P.cmax + c, 0, (size_t)nc * sizeof(unsigned long long), st);
+            if (ce != cudaSuccess) return (int)ce;
+            dim3 g1((unsigned)ceil_div(P.m, 4096), (unsigned)nc);
+            colmax_kernel<<<g1, 256, 0, st>>>(P.X, P.ld, P.m, c, P.cmax);
+            g_launch_count += 1;
         }
-#undef BCGS_SLICE
-        g_launch_count += 2;
-        for (int k = c; k < e; ++k) P.fresh[k] = 1;
+        const dim3 sgrid((unsigned)ceil_div(P.m, 128), (unsigned)ceil_div(nc, 16));
+        if (P.kd == 6)
+            slice_kernel<6><<<sgrid, 128, 0, st>>>(P.X, P.ld, P.m, c, nc, P.cmax, P.cexp, P.colstore, P.ldr,
+                                                   P.plane_col, P.rowstore, P.ldc, P.plane_row);
+        else
+            slice_kernel<7><<<sgrid, 128, 0, st>>>(P.X, P.ld, P.m, c, nc, P.cmax, P.cexp, P.colstore, P.ldr,
+                                                   P.plane_col, P.rowstore, P.ldc, P.plane_row);
+        g_launch_count += 1;
+        for (int k = c; k < e; ++k) { P.fresh[k] = 1; P.cmax_valid[k] = 0; }
         c = e;
     }
     return (int)cudaGetLastError();
@@ -770,6 +903,7 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     if (need > ws_bytes) return (int)cudaErrorInvalidValue;
     P.X = X; P.ld = ld; P.m = m; P.n = n; P.num_sms = num_sms;
     P.fresh.assign((size_t)n, 0);
+    P.cmax_valid.assign((size_t)n, 0);
     // The row store must hold finite values everywhere: the last K chunk of an
     // update reads columns past K + nc (multiplied by zero rows of the factor).
     if (P.zeroed_base != (const void*)P.rowstore || P.zeroed_bytes < (size_t)(P.plane_row * KD_MAX * 2)) {
@@ -794,10 +928,6 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
         if (!rc) rc = set_smem(update_tc_kernel<16, 7>, SmemLayout<16, 7>::BYTES);
         if (!rc) rc = set_smem(update_tc_kernel<32, 6>, SmemLayout<32, 6>::BYTES);
         if (!rc) rc = set_smem(update_tc_kernel<32, 7>, SmemLayout<32, 7>::BYTES);
-        if (!rc) rc = set_smem(slice_kernel<16, 6>, 6 * 16 * 256 * 2);
-        if (!rc) rc = set_smem(slice_kernel<16, 7>, 7 * 16 * 256 * 2);
-        if (!rc) rc = set_smem(slice_kernel<32, 6>, 6 * 32 * 256 * 2);
-        if (!rc) rc = set_smem(slice_kernel<32, 7>, 7 * 32 * 256 * 2);
         if (rc) return rc;
         attrs = true;
     }
@@ -805,7 +935,10 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
 }
 
 void split_mark_stale(int c0, int nc) {
-    for (int c = c0; c < c0 + nc && c < (int)g_plan.fresh.size(); ++c) g_plan.fresh[c] = 0;
+    for (int c = c0; c < c0 + nc && c < (int)g_plan.fresh.size(); ++c) {
+        g_plan.fresh[c] = 0;
+        g_plan.cmax_valid[c] = 0;
+    }
 }
 
 int split_error_word(int* out, cudaStream_t st) {
@@ -849,28 +982,22 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     return launch_gram_reduce(P.part, gp.rc, na, nb, out, ldo, st);
 }
 
-int launch_update_split(double* X, i64 ld, i64 m, int K, int c0, int nc, const double* S, int lds,
-                        const double* T, int ldt, char* ws, size_t ws_bytes, int num_sms, cudaStream_t st) {
-    (void)ws; (void)ws_bytes;
+// bdigit + the tensor-core product X[:, c0:c0+nc] = rowstore[:, 0:kin] * Bp, after the
+// caller has filled Bp/bmax.
+static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int num_sms, cudaStream_t st) {
     Plan& P = g_plan;
-    if (nc <= 0) return 0;
-    if (c0 != K || nc > 32 || X != P.X) return (int)cudaErrorInvalidValue;
-    int rc = ensure_fresh(0, K + nc, st);
-    if (rc) return rc;
     const int NB = nc <= 16 ? 16 : 32;
-    cudaError_t ce = cudaMemsetAsync(P.bmax, 0, 64 * sizeof(unsigned long long), st);
-    if (ce != cudaSuccess) return (int)ce;
-    const int kin = K + nc;
-    bbuild_kernel<<<(unsigned)ceil_div(kin, 64), 256, 0, st>>>(S, lds, T, ldt, K, nc, P.cexp, P.bfull,
-                                                                  (int)P.kpad, P.bmax);
     if (P.kd == 6)
-        bdigit_kernel<6><<<(unsigned)ceil_div(P.kpad, 256), 256, 0, st>>>(P.bfull, (int)P.kpad, K, nc, NB,
+        bdigit_kernel<6><<<(unsigned)ceil_div(P.kpad, 256), 256, 0, st>>>(P.bfull, (int)P.kpad, kin - nc, nc, NB,
                                                                            (int)P.kpad, P.bmax, P.fexp, P.bdig);
     else
-        bdigit_kernel<7><<<(unsigned)ceil_div(P.kpad, 256), 256, 0, st>>>(P.bfull, (int)P.kpad, K, nc, NB,
+        bdigit_kernel<7><<<(unsigned)ceil_div(P.kpad, 256), 256, 0, st>>>(P.bfull, (int)P.kpad, kin - nc, nc, NB,
                                                                            (int)P.kpad, P.bmax, P.fexp, P.bdig);
+    cudaError_t ce = cudaMemsetAsync(P.cmax + c0, 0, (size_t)nc * sizeof(unsigned long long), st);
+    if (ce != cudaSuccess) return (int)ce;
     UpdateParams up;
-    up.m = m; up.kin = kin; up.nc = nc; up.c0 = c0; up.ld = ld; up.X = X; up.fexp = P.fexp; up.err = P.err;
+    up.m = m; up.kin = kin; up.nc = nc; up.c0 = c0; up.ld = ld; up.X = X; up.fexp = P.fexp;
+    up.cmax = P.cmax; up.err = P.err;
     const int ntiles = (int)ceil_div(m, TILE_M);
     const int grid = ntiles < num_sms ? ntiles : num_sms;
 #define BCGS_UPD(NBT, KDT) \
@@ -881,9 +1008,42 @@ int launch_update_split(double* X, i64 ld, i64 m, int K, int c0, int nc, const d
         if (P.kd == 6) BCGS_UPD(32, 6); else BCGS_UPD(32, 7);
     }
 #undef BCGS_UPD
-    g_launch_count += 3;
-    for (int c = c0; c < c0 + nc; ++c) P.fresh[c] = 0;
+    g_launch_count += 2;
+    for (int c = c0; c < c0 + nc; ++c) { P.fresh[c] = 0; P.cmax_valid[c] = 1; }
     return (int)cudaGetLastError();
+}
+
+int launch_update_split(double* X, i64 ld, i64 m, int K, int c0, int nc, const double* S, int lds,
+                        const double* T, int ldt, char* ws, size_t ws_bytes, int num_sms, cudaStream_t st) {
+    (void)ws; (void)ws_bytes;
+    Plan& P = g_plan;
+    if (nc <= 0) return 0;
+    if (c0 != K || nc > 32 || X != P.X) return (int)cudaErrorInvalidValue;
+    int rc = ensure_fresh(0, K + nc, st);
+    if (rc) return rc;
+    cudaError_t ce = cudaMemsetAsync(P.bmax, 0, 64 * sizeof(unsigned long long), st);
+    if (ce != cudaSuccess) return (int)ce;
+    const int kin = K + nc;
+    bbuild_kernel<<<(unsigned)ceil_div(kin, 64), 256, 0, st>>>(S, lds, T, ldt, K, nc, P.cexp, P.bfull,
+                                                                  (int)P.kpad, P.bmax);
+    g_launch_count += 1;
+    return finish_update(X, ld, m, kin, c0, nc, num_sms, st);
+}
+
+int launch_fused_update_split(double* X, i64 ld, i64 m, int K, int s, int nz, const double* G, int ldg,
+                              const double* Ty, const double* Sp, int ldsp, const double* Ts, int num_sms,
+                              cudaStream_t st) {
+    Plan& P = g_plan;
+    const int kin = K + s + nz, nout = s + nz;
+    if (s > 16 || nz > 16 || nout > 32 || X != P.X) return (int)cudaErrorInvalidValue;
+    int rc = ensure_fresh(0, kin, st);
+    if (rc) return rc;
+    cudaError_t ce = cudaMemsetAsync(P.bmax, 0, 64 * sizeof(unsigned long long), st);
+    if (ce != cudaSuccess) return (int)ce;
+    bbuild_fused_kernel<<<(unsigned)ceil_div(kin, 64), 256, 0, st>>>(G, ldg, K, s, Ty, s, Sp, ldsp, Ts, nz, nz,
+                                                                        P.cexp, P.bfull, (int)P.kpad, P.bmax);
+    g_launch_count += 1;
+    return finish_update(X, ld, m, kin, K, nout, num_sms, st);
 }
 
 }  // namespace bcgs
