@@ -14,11 +14,12 @@
 // accumulator every 256 summation steps into two 64-bit integers; group g = 8
 // (weight 2^-48 relative) is summed in FP32.
 //
-// Two digit stores serve the two product shapes, both K-major for the tensor core:
-//   column store [plane][column][row]  (rows contiguous): A and B of the tall Gram
-//                                       X[:, 0:na]^T X[:, b0:b0+nb]  (sum over rows)
-//   row store    [plane][row][column]  (columns contiguous): A of the update
-//                                       [Q | X_k] * B  (sum over columns)
+// Two digit stores serve the two product shapes, both K-major for the tensor core
+// and chunked so that every 128 x 64 TMA tile is one contiguous 16 KB block of HBM:
+//   column store [plane][64-row chunk][column][64 rows]: A and B of the tall Gram
+//                X[:, 0:na]^T X[:, b0:b0+nb] (sum over rows)
+//   row store    [plane][64-column chunk][row][64 columns]: A of the update
+//                [Q | X_k] * B (sum over columns)
 // The update (X_k - Q S) T^{-1} is evaluated as one product
 //     [Q | X_k] * [-S T^{-1} ; T^{-1}]
 // with the column scales 2^{e_c} folded into the rows of the small right-hand
@@ -138,10 +139,9 @@ __global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c
 // along the rows. Small CTAs keep many loads in flight per SM.
 template <int KD>
 __global__ void __launch_bounds__(128, 4)
-slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int c0, int nc,
+slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
              const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
-             unsigned short* __restrict__ colstore, i64 ldr, i64 plane_col,
-             unsigned short* __restrict__ rowstore, i64 ldc, i64 plane_row) {
+             unsigned short* __restrict__ colstore, i64 nrc, unsigned short* __restrict__ rowstore, i64 ncc) {
     constexpr int CG = 16;                   // columns per CTA (one 32-byte row-store sector)
     __shared__ __align__(16) unsigned short sdig[KD][CG][128];
     const int t = threadIdx.x;
@@ -166,36 +166,44 @@ slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int c0, int nc,
             sdig[i][j + 1][t] = b1;
         }
     }
+    // Row store: element (r, c) of plane i at ((i*ncc + c/64)*m + r)*64 + c%64.
     if (r < m) {
-        const bool vec = (g + CG <= nc) && (((c0 + g) & 7) == 0) && ((ldc & 7) == 0);
+        const int cb = c0 + g;
+        const bool vec = (g + CG <= nc) && ((cb & 15) == 0);   // 16 columns in one 64-column chunk
 #pragma unroll
         for (int i = 0; i < KD; ++i) {
-            unsigned short* dst = rowstore + (i64)i * plane_row + r * ldc + c0 + g;
             if (vec) {
+                unsigned short* dst = rowstore + (((i64)i * ncc + cb / 64) * m + r) * 64 + (cb & 63);
                 uint4* d4 = reinterpret_cast<uint4*>(dst);
                 d4[0] = make_uint4(packed[i][0], packed[i][1], packed[i][2], packed[i][3]);
                 d4[1] = make_uint4(packed[i][4], packed[i][5], packed[i][6], packed[i][7]);
             } else {
 #pragma unroll
-                for (int j = 0; j < CG; ++j)
-                    if (g + j < nc) dst[j] = (unsigned short)((packed[i][j / 2] >> (16 * (j & 1))) & 0xFFFFu);
+                for (int j = 0; j < CG; ++j) {
+                    const int c = cb + j;
+                    if (g + j < nc)
+                        rowstore[(((i64)i * ncc + c / 64) * m + r) * 64 + (c & 63)] =
+                            (unsigned short)((packed[i][j / 2] >> (16 * (j & 1))) & 0xFFFFu);
+                }
             }
         }
     }
     __syncthreads();
-    // Column store: per (plane, column) 128 rows = 16 pieces of 16 bytes.
-    const bool full = (r0 + 128 <= m) && ((ldr & 7) == 0);
+    // Column store: element (r, c) of plane i at ((i*nrc + r/64)*n + c)*64 + r%64; per
+    // (plane, column) the CTA's 128 rows are two 128-byte runs = 16 pieces of 16 bytes.
+    const bool full = (r0 + 128 <= m);
     for (int e = t; e < KD * CG * 16; e += 128) {
         const int piece = e & 15, ij = e >> 4;
         const int i = ij / CG, j = ij % CG;
         if (g + j >= nc) continue;
-        unsigned short* dst = colstore + (i64)i * plane_col + (i64)(c0 + g + j) * ldr + r0 + piece * 8;
+        const i64 rr = r0 + piece * 8;
+        unsigned short* dst = colstore + (((i64)i * nrc + rr / 64) * n + (c0 + g + j)) * 64 + (rr & 63);
         const unsigned short* src = &sdig[i][j][piece * 8];
         if (full) {
             *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(src);
         } else {
             for (int q = 0; q < 8; ++q)
-                if (r0 + piece * 8 + q < m) dst[q] = src[q];
+                if (rr + q < m) dst[q] = src[q];
         }
     }
 }
@@ -441,19 +449,20 @@ __device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapA, const CUt
                                               uint8_t* sB, Bars* bars, Ring& ra, Ring& rb, CoordFn coords,
                                               int item, int ch, volatile int* abort, int* err) {
     constexpr int B_SLOT = SmemLayout<NB, KD>::B_SLOT;
-    int ax, ay, bx, by;
-    coords(item, ch, ax, ay, bx, by);
+    // Plane p of A is at (ax, ay, az + p*azs); plane p of B at (bx, by, bz + p*bzs).
+    int ax, ay, az, azs, bx, by, bz, bzs;
+    coords(item, ch, ax, ay, az, azs, bx, by, bz, bzs);
     if (!tc::mbar_wait(&bars->b_empty[rb.slot], rb.phase ^ 1u, abort, err, 11)) return false;
     tc::mbar_expect_tx(&bars->b_full[rb.slot], (uint32_t)B_SLOT);
 #pragma unroll
     for (int j = 0; j < KD; ++j)
-        tc::tma_load_3d(sB + rb.slot * B_SLOT + j * NB * KCH * 2, mapB, &bars->b_full[rb.slot], bx, by, j);
+        tc::tma_load_3d(sB + rb.slot * B_SLOT + j * NB * KCH * 2, mapB, &bars->b_full[rb.slot], bx, by, bz + j * bzs);
     rb.advance(RB);
 #pragma unroll
     for (int i = 0; i < KD; ++i) {
         if (!tc::mbar_wait(&bars->a_empty[ra.slot], ra.phase ^ 1u, abort, err, 12)) return false;
         tc::mbar_expect_tx(&bars->a_full[ra.slot], (uint32_t)A_SLOT);
-        tc::tma_load_3d(sA + ra.slot * A_SLOT, mapA, &bars->a_full[ra.slot], ax, ay, i);
+        tc::tma_load_3d(sA + ra.slot * A_SLOT, mapA, &bars->a_full[ra.slot], ax, ay, az + i * azs);
         ra.advance(RA);
     }
     return true;
@@ -515,7 +524,7 @@ __device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint
 // X[r, c] X[r, b0 + j] for c in the M-block, j in the N-group.
 // ---------------------------------------------------------------------------
 struct GramParams {
-    int na, nb, b0;
+    int na, nb, b0, nrc;
     i64 m;
     int numMB, numNG, rc;
     i64 rows_per;   // multiple of WIN*KCH
@@ -547,11 +556,10 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     const int nchunks = r1 > r0 ? (int)ceil_div(r1 - r0, KCH) : 0;
     const int nwin = (nchunks + WIN - 1) / WIN;
 
-    auto coords = [&](int, int ch, int& ax, int& ay, int& bx, int& by) {
-        ax = (int)(r0 + (i64)ch * KCH);
-        ay = mb * TILE_M;
-        bx = ax;
-        by = p.b0 + ng * NB;
+    auto coords = [&](int, int ch, int& ax, int& ay, int& az, int& azs, int& bx, int& by, int& bz, int& bzs) {
+        const int rc = (int)((r0 + (i64)ch * KCH) / KCH);   // 64-row chunk of the column store
+        ax = 0; ay = mb * TILE_M; az = rc; azs = p.nrc;
+        bx = 0; by = p.b0 + ng * NB; bz = rc; bzs = p.nrc;
     };
 
     if (warp == 0) {
@@ -628,6 +636,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
 // ---------------------------------------------------------------------------
 struct UpdateParams {
     i64 m;
+    int ncc;      // 64-column chunks of the row store
     int kin;      // K + nc (inner length)
     int nc, c0;
     i64 ld;
@@ -657,11 +666,9 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     if (threadIdx.x < 32) s_cmax[threadIdx.x] = 0ULL;
     __syncthreads();
 
-    auto coords = [&](int tile, int ch, int& ax, int& ay, int& bx, int& by) {
-        ax = ch * KCH;
-        ay = tile * TILE_M;
-        bx = ch * KCH;
-        by = 0;
+    auto coords = [&](int tile, int ch, int& ax, int& ay, int& az, int& azs, int& bx, int& by, int& bz, int& bzs) {
+        ax = 0; ay = tile * TILE_M; az = ch; azs = p.ncc;   // 64-column chunk of the row store
+        bx = ch * KCH; by = 0; bz = 0; bzs = 1;
     };
 
     if (warp == 0) {
@@ -784,7 +791,7 @@ struct Plan {
     double* X = nullptr;
     i64 ld = 0, m = 0;
     int n = 0, num_sms = kNumSMsDefault;
-    i64 ldr = 0, ldc = 0, plane_col = 0, plane_row = 0, kpad = 0;
+    i64 nrc = 0, ncc = 0, kpad = 0;   // 64-row chunks (column store), 64-column chunks (row store)
     // device buffers (carved from the workspace)
     unsigned short *colstore = nullptr, *rowstore = nullptr, *bdig = nullptr;
     int *cexp = nullptr, *fexp = nullptr, *err = nullptr;
@@ -796,8 +803,9 @@ struct Plan {
     int kd = 7;
     std::vector<char> fresh;
     std::vector<char> cmax_valid;   // cmax[c] already holds max |X[:, c]| (set by the update)
-    const void* zeroed_base = nullptr;
-    size_t zeroed_bytes = 0;
+    const void* zeroed_base = nullptr;   // stores zeroed for this base and shape
+    i64 zeroed_m = -1;
+    int zeroed_n = -1;
 };
 Plan g_plan;
 
@@ -828,10 +836,9 @@ i64 gram_part_doubles(i64 m, int n, int s, int num_sms) {
 
 size_t layout_bytes(i64 m, int n, int s, int num_sms, Plan* out, char* base) {
     Carve cv{base};
-    const i64 ldr = round_up(m, 64), ldc = round_up(n, 64), kpad = round_up(n, 64);
-    const i64 plane_col = (i64)n * ldr, plane_row = m * ldc;
-    unsigned short* col = cv.take<unsigned short>(plane_col * KD_MAX);
-    unsigned short* row = cv.take<unsigned short>(plane_row * KD_MAX);
+    const i64 nrc = ceil_div(m, 64), ncc = ceil_div(n, 64), kpad = round_up(n, 64);
+    unsigned short* col = cv.take<unsigned short>((i64)KD_MAX * nrc * n * 64);
+    unsigned short* row = cv.take<unsigned short>((i64)KD_MAX * ncc * m * 64);
     unsigned short* bd = cv.take<unsigned short>((i64)KD_MAX * 32 * kpad);
     int* cexp = cv.take<int>(n + 64);
     int* fexp = cv.take<int>(64);
@@ -842,8 +849,7 @@ size_t layout_bytes(i64 m, int n, int s, int num_sms, Plan* out, char* base) {
     const i64 pd = gram_part_doubles(m, n, s, num_sms);
     double* part = cv.take<double>(pd);
     if (out) {
-        out->ldr = ldr; out->ldc = ldc; out->kpad = kpad;
-        out->plane_col = plane_col; out->plane_row = plane_row;
+        out->nrc = nrc; out->ncc = ncc; out->kpad = kpad;
         out->colstore = col; out->rowstore = row; out->bdig = bd;
         out->cexp = cexp; out->fexp = fexp; out->err = err;
         out->cmax = cmax; out->bmax = bmax; out->bfull = bfull; out->part = part;
@@ -869,11 +875,11 @@ int ensure_fresh(int c_begin, int c_end, cudaStream_t st) {
         }
         const dim3 sgrid((unsigned)ceil_div(P.m, 128), (unsigned)ceil_div(nc, 16));
         if (P.kd == 6)
-            slice_kernel<6><<<sgrid, 128, 0, st>>>(P.X, P.ld, P.m, c, nc, P.cmax, P.cexp, P.colstore, P.ldr,
-                                                   P.plane_col, P.rowstore, P.ldc, P.plane_row);
+            slice_kernel<6><<<sgrid, 128, 0, st>>>(P.X, P.ld, P.m, P.n, c, nc, P.cmax, P.cexp, P.colstore, P.nrc,
+                                                   P.rowstore, P.ncc);
         else
-            slice_kernel<7><<<sgrid, 128, 0, st>>>(P.X, P.ld, P.m, c, nc, P.cmax, P.cexp, P.colstore, P.ldr,
-                                                   P.plane_col, P.rowstore, P.ldc, P.plane_row);
+            slice_kernel<7><<<sgrid, 128, 0, st>>>(P.X, P.ld, P.m, P.n, c, nc, P.cmax, P.cexp, P.colstore, P.nrc,
+                                                   P.rowstore, P.ncc);
         g_launch_count += 1;
         for (int k = c; k < e; ++k) { P.fresh[k] = 1; P.cmax_valid[k] = 0; }
         c = e;
@@ -904,19 +910,27 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     P.X = X; P.ld = ld; P.m = m; P.n = n; P.num_sms = num_sms;
     P.fresh.assign((size_t)n, 0);
     P.cmax_valid.assign((size_t)n, 0);
-    // The row store must hold finite values everywhere: the last K chunk of an
-    // update reads columns past K + nc (multiplied by zero rows of the factor).
-    if (P.zeroed_base != (const void*)P.rowstore || P.zeroed_bytes < (size_t)(P.plane_row * KD_MAX * 2)) {
-        cudaError_t ce = cudaMemsetAsync(P.rowstore, 0, (size_t)P.plane_row * KD_MAX * 2, st);
+    // Both stores are zeroed whenever the workspace or the shape changes. The
+    // chunk padding the slicing never writes (rows past m in the last 64-row chunk
+    // of the column store, columns past n in the last 64-column chunk of the row
+    // store) lies inside the TMA boxes and must read as zero, and the rest of the
+    // row store must hold digits or zeros (never bytes of another layout) because
+    // the last K chunk of an update reads columns past K + nc, multiplied by zero
+    // rows of the factor. Repeated runs of one shape keep their zeroed padding.
+    if (P.zeroed_base != (const void*)P.colstore || P.zeroed_m != m || P.zeroed_n != n) {
+        cudaError_t ce = cudaMemsetAsync(P.colstore, 0, (size_t)KD_MAX * P.nrc * 64 * n * 2, st);
+        if (ce == cudaSuccess) ce = cudaMemsetAsync(P.rowstore, 0, (size_t)KD_MAX * P.ncc * 64 * m * 2, st);
         if (ce != cudaSuccess) return (int)ce;
-        P.zeroed_base = P.rowstore;
-        P.zeroed_bytes = (size_t)P.plane_row * KD_MAX * 2;
+        P.zeroed_base = P.colstore;
+        P.zeroed_m = m;
+        P.zeroed_n = n;
     }
     cudaError_t ce = cudaMemsetAsync(P.err, 0, sizeof(int), st);
     if (ce != cudaSuccess) return (int)ce;
-    int rc = make_map3(&P.map_col_a, P.colstore, m, n, KD_MAX, P.ldr, P.plane_col, TILE_M);
-    if (!rc) rc = make_map3(&P.map_col_b, P.colstore, m, n, KD_MAX, P.ldr, P.plane_col, 32);
-    if (!rc) rc = make_map3(&P.map_row_a, P.rowstore, n, m, KD_MAX, P.ldc, P.plane_row, TILE_M);
+    // Chunked stores as 3-D tensors {64, columns or rows, plane x chunk}.
+    int rc = make_map3(&P.map_col_a, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, TILE_M);
+    if (!rc) rc = make_map3(&P.map_col_b, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 32);
+    if (!rc) rc = make_map3(&P.map_row_a, P.rowstore, 64, m, KD_MAX * P.ncc, 64, m * 64, TILE_M);
     if (!rc) rc = make_map3(&P.map_bdig16, P.bdig, P.kpad, 16, KD_MAX, P.kpad, 16 * P.kpad, 16);
     if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
     if (rc) return rc;
@@ -966,6 +980,7 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     gp.rc = num_sms / mbn > 0 ? num_sms / mbn : 1;
     gp.rows_per = round_up(ceil_div(m, gp.rc), (i64)WIN * KCH);
     gp.rc = (int)ceil_div(m, gp.rows_per);
+    gp.nrc = (int)P.nrc;
     gp.cexp = P.cexp;
     gp.part = P.part;
     gp.err = P.err;
@@ -996,6 +1011,7 @@ static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int 
     cudaError_t ce = cudaMemsetAsync(P.cmax + c0, 0, (size_t)nc * sizeof(unsigned long long), st);
     if (ce != cudaSuccess) return (int)ce;
     UpdateParams up;
+    up.ncc = (int)P.ncc;
     up.m = m; up.kin = kin; up.nc = nc; up.c0 = c0; up.ld = ld; up.X = X; up.fexp = P.fexp;
     up.cmax = P.cmax; up.err = P.err;
     const int ntiles = (int)ceil_div(m, TILE_M);
