@@ -138,14 +138,15 @@ def alg_flops_p1s(m: int, n: int, s: int) -> float:
     return 4.0 * m * n * n + 8.0 * m * n * s
 
 
-def traffic_from_profiles(kernel_class: str):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary
-    (profiles/traffic.json), or None when no capture has been summarized."""
+def traffic_ratio(kernel_class: str):
+    """DRAM traffic / algorithmic bytes of a kernel class, from the committed ncu
+    summary (profiles/traffic.json), or None when no capture has been summarized."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(p):
         return None
     try:
-        return json.load(open(p)).get(kernel_class)
+        v = json.load(open(p)).get(kernel_class)
+        return float(v) if v is not None else None
     except Exception:
         return None
 
@@ -346,10 +347,13 @@ def run_ours(args, rank, world, local_rank):
         achieved = pc["bytes"] / (pc["ms"] * 1e-3) / 1e9 if pc["ms"] > 0 else 0.0
         kd = 7
         tensor_tflops = pc["flops"] * kd * (kd + 1) / 2 / (pc["ms"] * 1e-3) / 1e12 if pc["ms"] > 0 else 0.0
+        ratio = traffic_ratio(dom)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic_from_profiles(dom),
+                "frac": round(achieved / peak, 4),
+                "traffic": round(ratio * pc["bytes"] / launches) if ratio is not None else None,
+                "traffic_note": "bytes per launch = ncu DRAM/algorithmic ratio (profiles/traffic.json) x algorithmic bytes per launch",
                 "kernel": {"gram": "gram_tc_kernel<7> + gram_reduce",
-                           "update": "bbuild + bdigit + update_tc_kernel<16,7>"}[dom],
+                           "update": "bbuild_fused + bdigit + update_tc_kernel<32,7> (fused Q_k/U_k+1 pass)"}[dom],
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
                 "launch_ms": round(pc["ms"] / launches, 4),
                 "bytes_per_launch": round(pc["bytes"] / launches),
