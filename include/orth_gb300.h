@@ -73,6 +73,13 @@ int orth_gb300_bcgsi2P1s_dev_noalloc(int m, int n, int s, double *dX, long long 
  */
 int orth_gb300_set_host_precision(int precision);
 
+/*
+ * Diagnostic of the split-precision kernels: the last nonzero error word, i.e. the
+ * code of a bounded wait that ran out (for the operand-ring waits, code + 100 *
+ * ring slot), or 0 if none has.
+ */
+int orth_gb300_last_split_error(void);
+
 /* 1 if the split-precision mode handles (m, n, s) (s <= 32), else 0. */
 int orth_gb300_split_supported(int m, int n, int s);
 

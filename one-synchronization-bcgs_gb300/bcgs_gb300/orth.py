@@ -77,6 +77,8 @@ def load(path: str | None = None):
     lib.orth_gb300_bcgsi2P1s_dev_noalloc.restype = ctypes.c_int
     lib.orth_gb300_set_host_precision.argtypes = [ctypes.c_int]
     lib.orth_gb300_set_host_precision.restype = ctypes.c_int
+    lib.orth_gb300_last_split_error.argtypes = []
+    lib.orth_gb300_last_split_error.restype = ctypes.c_int
     lib.orth_gb300_split_supported.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.orth_gb300_split_supported.restype = ctypes.c_int
     lib.orth_gb300_gram_dev.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -162,6 +164,11 @@ def bcgsi2P1s_dev_noalloc(m: int, n: int, s: int, x_ptr: int, ldx: int, r_ptr: i
 def set_host_precision(precision: int) -> int:
     """Precision of the orth.h entry points (FP64, SPLIT_BF16, SPLIT_BF16_FAST)."""
     return int(load().orth_gb300_set_host_precision(precision))
+
+
+def last_split_error() -> int:
+    """Code of the last bounded wait of the split kernels that ran out (0 if none)."""
+    return int(load().orth_gb300_last_split_error())
 
 
 def split_supported(m: int, n: int, s: int) -> bool:

@@ -711,6 +711,8 @@ int orth_gb300_set_host_precision(int precision) {
     return 0;
 }
 
+int orth_gb300_last_split_error(void) { return split_last_error(); }
+
 int orth_gb300_split_supported(int m, int n, int s) { return split_supported(m, n, s) ? 1 : 0; }
 
 int orth_gb300_gram_dev(int m, int na, int b0, int nb, const double* dX, long long ldX, double* dC,

@@ -26,6 +26,9 @@ void split_mark_stale(int c0, int nc);
 // Reads (and waits for) the split kernels' error word: 0, or the code of a wait
 // that ran out.
 int split_error_word(int* out, cudaStream_t st);
+// Last nonzero error word seen: the code of the bounded wait that ran out (for the
+// A-ring waits, code + 100 * ring slot).
+int split_last_error();
 // Same contracts as launch_gram_fp64 / launch_update_fp64 (the update requires
 // c0 == K and nc <= 32).
 int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, double* out, int ldo,

@@ -460,7 +460,7 @@ __device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapA, const CUt
     rb.advance(RB);
 #pragma unroll
     for (int i = 0; i < KD; ++i) {
-        if (!tc::mbar_wait(&bars->a_empty[ra.slot], ra.phase ^ 1u, abort, err, 12)) return false;
+        if (!tc::mbar_wait(&bars->a_empty[ra.slot], ra.phase ^ 1u, abort, err, 12 + 100 * ra.slot)) return false;
         tc::mbar_expect_tx(&bars->a_full[ra.slot], (uint32_t)A_SLOT);
         tc::tma_load_3d(sA + ra.slot * A_SLOT, mapA, &bars->a_full[ra.slot], ax, ay, az + i * azs);
         ra.advance(RA);
@@ -478,7 +478,7 @@ __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uin
     const uint32_t b_addr = tc::smem_u32(sB + rb.slot * B_SLOT);
 #pragma unroll
     for (int i = 0; i < KD; ++i) {
-        if (!tc::mbar_wait(&bars->a_full[ra.slot], ra.phase, abort, err, 22)) return false;
+        if (!tc::mbar_wait(&bars->a_full[ra.slot], ra.phase, abort, err, 22 + 100 * ra.slot)) return false;
         tc::tc_fence_after();
         const uint32_t a_addr = tc::smem_u32(sA + ra.slot * A_SLOT);
         const uint32_t idesc = tc::idesc_bf16_f32(TILE_M, NB * (KD - i));
@@ -955,11 +955,16 @@ void split_mark_stale(int c0, int nc) {
     }
 }
 
+int g_last_split_error = 0;
+
 int split_error_word(int* out, cudaStream_t st) {
     cudaError_t ce = cudaMemcpyAsync(out, g_plan.err, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce == cudaSuccess && *out) g_last_split_error = *out;
     return (int)ce;
 }
+
+int split_last_error() { return g_last_split_error; }
 
 int split_prepare(int c_end, cudaStream_t st) { return ensure_fresh(0, c_end, st); }
 
