@@ -92,6 +92,24 @@ int orth_gb300_split_supported(int m, int n, int s);
 int orth_gb300_gram_dev(int m, int na, int b0, int nb, const double *dX, long long ldX,
                         double *dC, int ldc, int precision, void *stream);
 
+/*
+ * Accuracy of a finished QR, on the device: the GPU form of the reference's
+ * test_orth_accuracy (SRC/util.c:36-75, which prints ||Q^T Q - I||_F and
+ * ||Q R - X||_F). dX: the original m x n matrix (ldX); dQ: the computed Q (ldQ);
+ * dR: the computed R (n x n, ldR; read as upper triangular).
+ *   out[0] = ||Q^T Q - I||_F, out[1] = ||Q R - X||_F, out[2] = ||X||_F.
+ * gram_precision selects how Q^T Q is formed: ORTH_GB300_FP64 (FP64 Gram kernel)
+ * or ORTH_GB300_SPLIT_BF16 (tensor-core digit Gram with exact accumulation; needs
+ * orth_gb300_split_supported(m, n, 16)). dE, if not NULL, receives the symmetric
+ * n x n error Q^T Q - I (lde >= n) for a 2-norm. Sums of squares are accumulated
+ * in double-double in a fixed order. Synchronizes the stream.
+ * Returns 0, 2 (invalid arguments), 3 (CUDA failure) or 4 (precision not
+ * available for this shape).
+ */
+int orth_gb300_accuracy_dev(int m, int n, const double *dX, long long ldX, const double *dQ, long long ldQ,
+                            const double *dR, int ldR, int gram_precision, double *dE, int lde, void *stream,
+                            double out[3]);
+
 /* Status of the last run through the orth.h entry points on this thread. */
 void orth_gb300_last_status(orth_gb300_status *status);
 

@@ -85,6 +85,11 @@ def load(path: str | None = None):
                                         ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p,
                                         ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     lib.orth_gb300_gram_dev.restype = ctypes.c_int
+    lib.orth_gb300_accuracy_dev.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong,
+                                            ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                            ctypes.POINTER(ctypes.c_double)]
+    lib.orth_gb300_accuracy_dev.restype = ctypes.c_int
     lib.orth_gb300_reserve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.orth_gb300_reserve.restype = ctypes.c_int
     lib.orth_gb300_release.argtypes = []
@@ -181,6 +186,22 @@ def gram_dev(m: int, na: int, b0: int, nb: int, x_ptr: int, ldx: int, c_ptr: int
     return int(load().orth_gb300_gram_dev(m, na, b0, nb, ctypes.c_void_p(x_ptr), ldx,
                                           ctypes.c_void_p(c_ptr), ldc, precision,
                                           ctypes.c_void_p(stream)))
+
+
+def accuracy_dev(m: int, n: int, x_ptr: int, ldx: int, q_ptr: int, ldq: int, r_ptr: int, ldr: int,
+                 gram_precision: int = SPLIT_BF16, e_ptr: int = 0, lde: int = 0, stream: int = 0):
+    """The reference's test_orth_accuracy (SRC/util.c:36-75) on device buffers.
+
+    Returns (rc, loo_fro, residual_fro, x_fro): ||Q^T Q - I||_F, ||Q R - X||_F and
+    ||X||_F. With e_ptr set, the symmetric n x n error Q^T Q - I is written there
+    (ld lde) for a 2-norm.
+    """
+    out = (ctypes.c_double * 3)()
+    rc = int(load().orth_gb300_accuracy_dev(m, n, ctypes.c_void_p(x_ptr), ldx, ctypes.c_void_p(q_ptr), ldq,
+                                            ctypes.c_void_p(r_ptr), ldr, gram_precision,
+                                            ctypes.c_void_p(e_ptr or None), lde or n, ctypes.c_void_p(stream),
+                                            out))
+    return rc, float(out[0]), float(out[1]), float(out[2])
 
 
 def sync_count(variant: str, n: int, s: int) -> int:

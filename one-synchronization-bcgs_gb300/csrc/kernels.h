@@ -41,4 +41,14 @@ i64 tsqr_workspace_doubles(i64 m, int nc);
 int launch_tsqr(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR, double* ws,
                 cudaStream_t st);
 
+// Accuracy metrics (the reference's test_orth_accuracy, SRC/util.c:36-75).
+// E (n x n, lde) = G - I from the upper triangle of the Gram G (ld ldg), mirrored;
+// out[0] = ||E||_F (double-double accumulation, fixed order).
+int launch_loo_finish(const double* G, int ldg, int n, double* E, int lde, double* out, cudaStream_t st);
+// out[1] = ||Q R - X||_F (R upper: entries below its diagonal are not read) and
+// out[2] = ||X||_F; part holds metrics_part_doubles(m, n) doubles.
+i64 metrics_part_doubles(i64 m, int n);
+int launch_residual(const double* X, i64 ldx, const double* Q, i64 ldq, i64 m, int n, const double* R, int ldr,
+                    double* part, double* out, cudaStream_t st);
+
 }  // namespace bcgs

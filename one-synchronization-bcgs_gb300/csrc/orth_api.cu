@@ -54,7 +54,7 @@ struct DevBuf {
 // Cached workspace (grow-only). The reference is not thread-safe either (it uses
 // MPI_COMM_WORLD collectives); calls are serialized by a mutex here.
 struct Context {
-    DevBuf part, gram, small, status, tsqr, hostX, hostR, split;
+    DevBuf part, gram, small, status, tsqr, hostX, hostR, split, metric;
     double* hostR_stage = nullptr;
     size_t hostR_stage_bytes = 0;
     cudaStream_t stream = nullptr;
@@ -743,6 +743,66 @@ int orth_gb300_gram_dev(int m, int na, int b0, int nb, const double* dX, long lo
             if (!rc && w) rc = (int)cudaErrorLaunchTimeout;
         }
     }
+    return rc ? 3 : 0;
+}
+
+int orth_gb300_accuracy_dev(int m, int n, const double* dX, long long ldX, const double* dQ, long long ldQ,
+                            const double* dR, int ldR, int gram_precision, double* dE, int lde, void* stream,
+                            double out[3]) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (m < 1 || n < 1 || !dX || !dQ || !dR || !out || ldX < m || ldQ < m || ldR < n) return 2;
+    if (dE && lde < n) return 2;
+    if (gram_precision != ORTH_GB300_FP64 && gram_precision != ORTH_GB300_SPLIT_BF16) return 4;
+    if (gram_precision == ORTH_GB300_SPLIT_BF16 && !split_supported(m, n, 16)) return 4;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (init_ctx()) return 3;
+    constexpr int GW = 32;   // Gram column group
+    // Layout of the metric buffer: G (n x n) | E (n x n, unless the caller's) |
+    // residual partials | out[3].
+    const i64 nn = (i64)n * n;
+    const i64 pd = metrics_part_doubles(m, n);
+    if (g_ctx.metric.ensure((size_t)(2 * nn + pd + 8) * sizeof(double))) return 3;
+    double* G = g_ctx.metric.as<double>();
+    double* E = dE ? dE : G + nn;
+    const int ldE = dE ? lde : n;
+    double* part = G + 2 * nn;
+    double* dout = part + pd;
+    int rc = 0;
+    if (gram_precision == ORTH_GB300_FP64) {
+        i64 need = 0;
+        for (int na = GW; na < n + GW; na += GW) {
+            const int a = na < n ? na : n;
+            const i64 v = (i64)gram_chunks_fp64(m, a, GW, g_ctx.num_sms) * a * GW;
+            if (v > need) need = v;
+        }
+        if (g_ctx.part.ensure((size_t)(need + 1024) * sizeof(double))) return 3;
+    } else {
+        if (g_ctx.split.ensure((size_t)split_workspace_bytes(m, n, 16, g_ctx.num_sms))) return 3;
+        rc = split_begin(const_cast<double*>(dQ), ldQ, m, n, 16, 7, g_ctx.split.as<char>(), g_ctx.split.bytes,
+                         g_ctx.num_sms, st);
+        if (rc) return 3;
+    }
+    // Upper block triangle of Q^T Q, one 32-column group at a time.
+    for (int c0 = 0; c0 < n && !rc; c0 += GW) {
+        const int nb = n - c0 < GW ? n - c0 : GW;
+        const int na = c0 + nb;
+        if (gram_precision == ORTH_GB300_FP64) {
+            const int chunks = gram_chunks_fp64(m, na, nb, g_ctx.num_sms);
+            rc = launch_gram_fp64(dQ, ldQ, m, 0, na, c0, nb, G + (i64)c0 * n, n, g_ctx.part.as<double>(), chunks, st);
+        } else {
+            rc = launch_gram_split(dQ, ldQ, m, na, c0, nb, G + (i64)c0 * n, n, g_ctx.split.as<char>(),
+                                   g_ctx.split.bytes, g_ctx.num_sms, st);
+        }
+    }
+    if (!rc && gram_precision != ORTH_GB300_FP64) {
+        int w = 0;
+        rc = split_error_word(&w, st);
+        if (!rc && w) rc = (int)cudaErrorLaunchTimeout;
+    }
+    if (!rc) rc = launch_loo_finish(G, n, n, E, ldE, dout, st);
+    if (!rc) rc = launch_residual(dX, ldX, dQ, ldQ, m, n, dR, ldR, part, dout, st);
+    if (!rc) rc = (int)cudaMemcpyAsync(out, dout, 3 * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (!rc) rc = (int)cudaStreamSynchronize(st);
     return rc ? 3 : 0;
 }
 
