@@ -59,6 +59,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--workload", choices=["qr", "batched"], default="qr",
+                    help="qr: one BCGSI+P-1S QR of m x n (default); batched: the batched form "
+                         "(--batch matrices of uneven m, s, p and kappa in one captured CUDA graph)")
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--batch-seed", type=int, default=2024)
+    ap.add_argument("--no-tune", action="store_true")
     return ap.parse_args()
 
 
@@ -399,6 +405,157 @@ def run_ours(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def batch_shapes(count: int, seed: int):
+    """The batched workload: m log-uniform in [2e3, 2e5], s in {4, 8, 16}, p uniform
+    in [2, 16], kappa log-uniform in [1e2, 1e10], all from one seed (n = s p)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    ms = np.exp(rng.uniform(np.log(2000), np.log(200000), count)).astype(np.int64)
+    ss = rng.choice([4, 8, 16], count)
+    ps = rng.integers(2, 17, count)
+    ks = np.exp(rng.uniform(np.log(1e2), np.log(1e10), count))
+    return [int(x) for x in ms], [int(s * p) for s, p in zip(ss, ps)], [int(x) for x in ss], [float(k) for k in ks]
+
+
+def run_batched(args, rank, world, local_rank):
+    """Batched BCGSI+P-1S: the whole batch as one captured CUDA graph per step."""
+    import numpy as np
+    import torch
+
+    from bcgs_gb300 import inputs, orth
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    orth.load()
+    ms, ns, ss, ks = batch_shapes(args.batch, args.batch_seed + rank)
+    free, _ = torch.cuda.mem_get_info(dev)
+    sizes = [m * n for m, n in zip(ms, ns)]
+    # Two copies of the batch (a resident pristine copy and the working one), the
+    # R factors and the plan's workspace must fit.
+    count = len(ms)
+    while count > 1 and 2 * 8 * sum(sizes[:count]) + 8 * sum(n * n for n in ns[:count]) + (8 << 30) > free:
+        count = int(count * 0.9)
+    ms, ns, ss, ks, sizes = ms[:count], ns[:count], ss[:count], ks[:count], sizes[:count]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    roffs = np.concatenate([[0], np.cumsum([n * n for n in ns])]).astype(np.int64)
+    X0 = torch.empty(int(offs[-1]), dtype=torch.float64, device=dev)
+    t_gen = time.perf_counter()
+    for b in range(count):
+        X0[int(offs[b]):int(offs[b + 1])].copy_(
+            inputs.graded_device(ms[b], ns[b], ks[b], seed=args.batch_seed * 100003 + b, device=str(dev)).reshape(-1))
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t_gen
+    X = X0.clone()
+    R = torch.zeros(int(roffs[-1]), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    xp = [X.data_ptr() + 8 * int(o) for o in offs[:-1]]
+    rp = [R.data_ptr() + 8 * int(o) for o in roffs[:-1]]
+    t_plan = time.perf_counter()
+    plan = orth.Batch(ms, ns, ss, xp, rp, tune=not args.no_tune, stream=sptr)
+    if plan.rc != 0:
+        raise RuntimeError(f"batch plan rc={plan.rc}")
+    torch.cuda.synchronize()
+    t_plan = time.perf_counter() - t_plan
+    info = plan.info()
+
+    def one(ev=None):
+        with torch.cuda.stream(stream):
+            X.copy_(X0)
+            R.zero_()
+            if ev is not None:
+                ev[0].record(stream)
+            if plan.run(sptr) != 0:
+                raise RuntimeError("batch run failed")
+            if ev is not None:
+                ev[1].record(stream)
+
+    for _ in range(max(0, args.warmup)):
+        one()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            one(evs[k])
+        torch.cuda.synchronize()
+    ms_run = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / args.steps, world, dev)
+    _, steps_bd, _, nbroken = plan.status()
+    total = count * world
+    value = total / (ms_run * 1e-3)
+
+    # Worst-case accuracy over the batch (the library's metrics kernels).
+    acc = {}
+    if not args.no_accuracy:
+        worst_loo, worst_res, worst_b = 0.0, 0.0, -1
+        for b in range(count):
+            m, n = ms[b], ns[b]
+            E = torch.empty((n, n), dtype=torch.float64, device=dev)
+            x0 = X0[int(offs[b]):int(offs[b + 1])]
+            gp = orth.SPLIT_BF16 if orth.split_supported(m, n, 16) else orth.FP64
+            rc, loo_f, res_f, x_f = orth.accuracy_dev(m, n, x0.data_ptr(), m, xp[b], m, rp[b], n, gp,
+                                                      E.data_ptr(), n, sptr)
+            if rc != 0:
+                raise RuntimeError(f"accuracy_dev rc={rc}")
+            loo2 = float(np.max(np.abs(np.linalg.eigvalsh(E.cpu().numpy()))))
+            if steps_bd[b] == 0 and loo2 > worst_loo:
+                worst_loo, worst_b = loo2, b
+            worst_res = max(worst_res, res_f / x_f if steps_bd[b] == 0 else 0.0)
+        acc = {"worst_loo_2": worst_loo, "worst_loo_matrix": {"m": ms[worst_b], "n": ns[worst_b],
+                                                               "s": ss[worst_b], "kappa": ks[worst_b]},
+               "worst_rel_residual": worst_res, "breakdowns": nbroken,
+               "metric": "orth_gb300_accuracy_dev per matrix (exact digit Gram, double-double sums)"}
+
+    flops = sum(4.0 * m * n * n + 8.0 * m * n * s for m, n, s in zip(ms, ns, ss))
+    peak = orth.fp64_peak_tflops()
+    achieved = flops / (ms_run * 1e-3) / 1e12
+    roof = {"bound": "fp64_pipe", "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
+            "frac": round(achieved / peak, 4), "traffic": None,
+            "note": "whole batch: algorithmic FLOPs (4mn^2 + 8mns per matrix) / graph time; peak = DFMA-loop probe"}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import bcgs_port
+        sample = list(range(0, count, max(1, count // 6)))[:6]
+        t0 = time.perf_counter()
+        for b in sample:
+            Xh = inputs.graded_host(ms[b], ns[b], ks[b], seed=b)
+            bcgs_port.run_variant("bcgsi2P1s", Xh, ns[b], ss[b])
+        dt = time.perf_counter() - t0
+        work = sum(sizes[b] * ns[b] for b in sample) / sum(sz * n for sz, n in zip(sizes, ns))
+        # The sample holds `work` of the batch's m n^2 work: the whole batch would take dt / work.
+        cpu = {"value": round(count / (dt / work), 3), "unit": "matrices/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{len(sample)} matrices of the batch through the oracle (numpy/OpenBLAS), time scaled "
+                         f"by the batch's m n^2 work"}
+    line = {
+        "metric": "matrices/s, batched BCGSI+P-1S (4096 X of m in [2e3,2e5], s in {4,8,16}, p in [2,16], "
+                  "kappa in [1e2,1e10])",
+        "value": round(value, 3), "unit": "matrices/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_run, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"batched bcgsi2P1s, {count} matrices (seed {args.batch_seed}), FP64, "
+                               f"one CUDA graph of {info['launches']} launches per step",
+                   "batch": count, "batch_requested": args.batch, "elements": int(offs[-1]),
+                   "tuned_panel_rows": {str(k): v for k, v in info["tuned"].items()},
+                   "l2": f"inputs ({8 * int(offs[-1]) / 1e9:.0f} GB) larger than L2; no flush",
+                   "restore": "X restored from a resident copy before each step, outside the timed interval",
+                   "setup_s": {"generate": round(t_gen, 1), "plan_tune_capture": round(t_plan, 2)}},
+        "accuracy": acc,
+        "gpu_launches": int(info["launches"] * args.steps),
+        "roofline": roof,
+        "clocks": clk.summary(),
+        "e2e": None,
+        "e2e_note": "the batch is 120 GB; a pinned host copy of it is not held, so no host-buffer run",
+        "cpu_baseline": cpu,
+    }
+    plan.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local_rank = dist_env()
@@ -409,7 +566,10 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl" if args.gpus > 1 else "gloo")
     try:
-        run_ours(args, rank, world, local_rank)
+        if args.workload == "batched":
+            run_batched(args, rank, world, local_rank)
+        else:
+            run_ours(args, rank, world, local_rank)
     finally:
         if world > 1:
             import torch.distributed as dist

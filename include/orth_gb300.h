@@ -110,6 +110,46 @@ int orth_gb300_accuracy_dev(int m, int n, const double *dX, long long ldX, const
                             const double *dR, int ldR, int gram_precision, double *dE, int lde, void *stream,
                             double out[3]);
 
+/*
+ * Rows per chunk of the FP64 Gram's fixed-order reduction (0 = the default policy,
+ * about four CTAs per SM). Results depend on the chunking only through the order
+ * of the final sum; a batched plan with the same chunk rows reproduces the
+ * single-matrix results bit for bit.
+ */
+void orth_gb300_set_gram_chunk_rows(long long rows);
+
+/*
+ * Batched form: many independent BCGSI+P-1S QRs (the reference's bcgsi2P1s on each
+ * matrix) run as one captured CUDA graph, one launch per stage for all matrices.
+ * Matrix b: dX[b] (m[b] x n[b], ldX[b] >= m[b], overwritten with Q), dR[b]
+ * (n[b] x n[b], ldR[b]; upper block triangle written), block size s[b] <= 16,
+ * n[b] >= 2 s[b], m[b] >= n[b]. Arrays are host arrays of count entries (ldX/ldR
+ * may be NULL: tight). precision: ORTH_GB300_FP64. variant: ORTH_GB300_BCGSI2P1S.
+ * flags: ORTH_GB300_BATCH_TUNE times the Gram's panel width and chunk rows per
+ * block size on the batch itself (reads X, writes only the plan's scratch).
+ * The plan owns its device workspace; runs must not overlap.
+ * Returns 0, 2 (invalid arguments), 3 (CUDA failure), 4 (variant/precision not
+ * available in batched form).
+ */
+typedef struct orth_gb300_batch orth_gb300_batch;
+#define ORTH_GB300_BATCH_TUNE 1
+int orth_gb300_batch_create(orth_gb300_batch **plan, int variant, int count, const int *m, const int *n,
+                            const int *s, double *const *dX, const long long *ldX, double *const *dR,
+                            const int *ldR, int precision, int flags, void *stream);
+/* Enqueue one run of the whole batch (a graph launch) on stream. */
+int orth_gb300_batch_run(orth_gb300_batch *plan, void *stream);
+/* Per-matrix Cholesky breakdown (step, info; 0 if none) of the last run; waits for the device. */
+int orth_gb300_batch_status(orth_gb300_batch *plan, int *breakdown_step, int *breakdown_info, int *nbroken);
+/* Kernel launches per run, device bytes held, graph nodes, and the tuned
+ * (panel width, chunk rows) for s <= 4, <= 8, <= 16 (tuned: 6 ints). */
+int orth_gb300_batch_info(const orth_gb300_batch *plan, long long *launches_per_run, long long *workspace_bytes,
+                          int *graph_nodes, int *tuned);
+void orth_gb300_batch_destroy(orth_gb300_batch *plan);
+/* The schedule without a GPU: stages, launches per run and device bytes a plan
+ * for these shapes would hold. */
+int orth_gb300_batch_dry_run(int count, const int *m, const int *n, const int *s, long long *stages,
+                             long long *launches_per_run, long long *workspace_bytes);
+
 /* Status of the last run through the orth.h entry points on this thread. */
 void orth_gb300_last_status(orth_gb300_status *status);
 

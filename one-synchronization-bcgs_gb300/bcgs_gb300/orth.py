@@ -90,6 +90,23 @@ def load(path: str | None = None):
                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                             ctypes.POINTER(ctypes.c_double)]
     lib.orth_gb300_accuracy_dev.restype = ctypes.c_int
+    lib.orth_gb300_set_gram_chunk_rows.argtypes = [ctypes.c_longlong]
+    lib.orth_gb300_set_gram_chunk_rows.restype = None
+    P_int, P_ll, P_vp = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_void_p)
+    lib.orth_gb300_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, P_int, P_int,
+                                            P_int, P_vp, P_ll, P_vp, P_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_void_p]
+    lib.orth_gb300_batch_create.restype = ctypes.c_int
+    lib.orth_gb300_batch_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.orth_gb300_batch_run.restype = ctypes.c_int
+    lib.orth_gb300_batch_status.argtypes = [ctypes.c_void_p, P_int, P_int, P_int]
+    lib.orth_gb300_batch_status.restype = ctypes.c_int
+    lib.orth_gb300_batch_info.argtypes = [ctypes.c_void_p, P_ll, P_ll, P_int, P_int]
+    lib.orth_gb300_batch_info.restype = ctypes.c_int
+    lib.orth_gb300_batch_destroy.argtypes = [ctypes.c_void_p]
+    lib.orth_gb300_batch_destroy.restype = None
+    lib.orth_gb300_batch_dry_run.argtypes = [ctypes.c_int, P_int, P_int, P_int, P_ll, P_ll, P_ll]
+    lib.orth_gb300_batch_dry_run.restype = ctypes.c_int
     lib.orth_gb300_reserve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.orth_gb300_reserve.restype = ctypes.c_int
     lib.orth_gb300_release.argtypes = []
@@ -202,6 +219,74 @@ def accuracy_dev(m: int, n: int, x_ptr: int, ldx: int, q_ptr: int, ldq: int, r_p
                                             ctypes.c_void_p(e_ptr or None), lde or n, ctypes.c_void_p(stream),
                                             out))
     return rc, float(out[0]), float(out[1]), float(out[2])
+
+
+def set_gram_chunk_rows(rows: int) -> None:
+    """Rows per FP64 Gram chunk (0 restores the default chunking policy)."""
+    load().orth_gb300_set_gram_chunk_rows(int(rows))
+
+
+BATCH_TUNE = 1
+
+
+def _int_array(v):
+    return (ctypes.c_int * len(v))(*[int(x) for x in v])
+
+
+def batch_dry_run(ms, ns, ss) -> dict:
+    """Stages, launches per run and device bytes of a batched plan (no GPU needed)."""
+    st, la, wb = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_longlong(0)
+    rc = int(load().orth_gb300_batch_dry_run(len(ms), _int_array(ms), _int_array(ns), _int_array(ss),
+                                             ctypes.byref(st), ctypes.byref(la), ctypes.byref(wb)))
+    return {"rc": rc, "stages": st.value, "launches": la.value, "bytes": wb.value}
+
+
+class Batch:
+    """A batched BCGSI+P-1S plan over device buffers (orth_gb300_batch_*).
+
+    x_ptrs[b]: device pointer of X_b (m x n column-major, ld ldx[b]); r_ptrs[b]:
+    device pointer of R_b (n x n, ld ldr[b]). The plan captures the whole batch
+    in one CUDA graph at creation; run() replays it.
+    """
+
+    def __init__(self, ms, ns, ss, x_ptrs, r_ptrs, ldx=None, ldr=None, precision=FP64, tune=True,
+                 stream: int = 0, variant: str = "bcgsi2P1s"):
+        lib = load()
+        self.count = len(ms)
+        self._h = ctypes.c_void_p(0)
+        xs = (ctypes.c_void_p * self.count)(*x_ptrs)
+        rs = (ctypes.c_void_p * self.count)(*r_ptrs)
+        lx = (ctypes.c_longlong * self.count)(*(ldx if ldx is not None else ms))
+        lr = _int_array(ldr if ldr is not None else ns)
+        self.rc = int(lib.orth_gb300_batch_create(ctypes.byref(self._h), VARIANT_ID[variant], self.count,
+                                                  _int_array(ms), _int_array(ns), _int_array(ss), xs, lx, rs, lr,
+                                                  precision, BATCH_TUNE if tune else 0, ctypes.c_void_p(stream)))
+
+    def run(self, stream: int = 0) -> int:
+        return int(load().orth_gb300_batch_run(self._h, ctypes.c_void_p(stream)))
+
+    def status(self):
+        steps, infos, nb = (ctypes.c_int * self.count)(), (ctypes.c_int * self.count)(), ctypes.c_int(0)
+        rc = int(load().orth_gb300_batch_status(self._h, steps, infos, ctypes.byref(nb)))
+        return rc, list(steps), list(infos), nb.value
+
+    def info(self) -> dict:
+        la, wb, gn = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_int(0)
+        tuned = (ctypes.c_int * 6)()
+        load().orth_gb300_batch_info(self._h, ctypes.byref(la), ctypes.byref(wb), ctypes.byref(gn), tuned)
+        return {"launches": la.value, "bytes": wb.value, "graph_nodes": gn.value,
+                "tuned": {4: (tuned[0], tuned[1]), 8: (tuned[2], tuned[3]), 16: (tuned[4], tuned[5])}}
+
+    def close(self) -> None:
+        if self._h:
+            load().orth_gb300_batch_destroy(self._h)
+            self._h = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def sync_count(variant: str, n: int, s: int) -> int:

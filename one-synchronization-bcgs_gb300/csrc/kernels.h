@@ -15,6 +15,8 @@ extern long long g_launch_count;
 // C (na x nb, ld ldo) = X[:, a0:a0+na]^T X[:, b0:b0+nb] over m rows, FP64, with a
 // fixed-order two-stage reduction through `part` (nchunks * na * nb doubles).
 int gram_chunks_fp64(i64 m, int na, int nb, int num_sms);
+// Rows per chunk forced by orth_gb300_set_gram_chunk_rows (0: default policy).
+extern long long g_gram_chunk_rows;
 int launch_gram_fp64(const double* X, i64 ld, i64 m, int a0, int na, int b0, int nb,
                      double* out, int ldo, double* part, int nchunks, cudaStream_t st);
 

@@ -746,6 +746,11 @@ int orth_gb300_gram_dev(int m, int na, int b0, int nb, const double* dX, long lo
     return rc ? 3 : 0;
 }
 
+void orth_gb300_set_gram_chunk_rows(long long rows) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    g_gram_chunk_rows = rows > 0 ? rows : 0;
+}
+
 int orth_gb300_accuracy_dev(int m, int n, const double* dX, long long ldX, const double* dQ, long long ldQ,
                             const double* dR, int ldR, int gram_precision, double* dE, int lde, void* stream,
                             double out[3]) {

@@ -8,6 +8,7 @@
 // Work here is O(K s^2) per step, negligible next to the tall passes, but it
 // sits on the critical path, so every step keeps it on the device: no host
 // round trip between the synchronizations.
+#include "batched.h"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -59,10 +60,12 @@ __device__ int chol_upper_shared(double* a, int nz) {
 // T(nz x nz, ld ldt) = chol_upper(Om(nz x nz, ld ldom) - A(k x nz, ld lda)^T A).
 // Only the upper triangle of Om is read; T's strictly lower part is zeroed
 // (dlaset 'L' + dlacpy 'U' + dpotrf 'U'). A may be null when k == 0.
-__global__ void __launch_bounds__(SM_THREADS)
-pyth_chol_kernel(const double* __restrict__ Om, int ldom, const double* __restrict__ A, int lda,
-                 int k, int nz, double* __restrict__ T, int ldt, int* __restrict__ status, int step) {
-    __shared__ double a[SMAX * SMAX];
+// Body shared by the single and batched kernels; `a` is SMAX*SMAX doubles of shared
+// memory. Starts and ends with a CTA barrier, so the caller may reuse `a`.
+__device__ void pyth_chol_body(const double* __restrict__ Om, int ldom, const double* __restrict__ A, int lda,
+                               int k, int nz, double* __restrict__ T, int ldt, int* __restrict__ status, int step,
+                               double* __restrict__ a) {
+    __syncthreads();
     for (int e = threadIdx.x; e < nz * nz; e += blockDim.x) {
         int i = e % nz, j = e / nz;
         double v = 0.0;
@@ -82,16 +85,25 @@ pyth_chol_kernel(const double* __restrict__ Om, int ldom, const double* __restri
         status[0] = step;
         status[1] = info;
     }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(SM_THREADS)
+pyth_chol_kernel(const double* __restrict__ Om, int ldom, const double* __restrict__ A, int lda,
+                 int k, int nz, double* __restrict__ T, int ldt, int* __restrict__ status, int step) {
+    __shared__ double a[SMAX * SMAX];
+    pyth_chol_body(Om, ldom, A, lda, k, nz, T, ldt, status, step, a);
 }
 
 // Scol(mScol x nZ, ld ldsc), mScol = mZ + s, from the last reduced Gram G (ld ldg):
 //   Scol = G[0:mScol, s:s+nZ]
 //   Scol[mZ:mScol] -= G[0:mZ, 0:s]^T G[0:mZ, s:s+nZ]
 //   Scol[mZ:mScol]  = Ydiag^{-T} Scol[mZ:mScol]       (dtrsm 'L','U','T','N')
-__global__ void __launch_bounds__(SM_THREADS)
-scol_kernel(const double* __restrict__ G, int ldg, int mZ, int s, int nZ,
-            const double* __restrict__ Yd, int ldy, double* __restrict__ Scol, int ldsc) {
-    extern __shared__ double dsm[];
+// Body shared by the single and batched kernels; dsm is SMAX*(nZ+s) doubles.
+__device__ void scol_body(const double* __restrict__ G, int ldg, int mZ, int s, int nZ,
+                          const double* __restrict__ Yd, int ldy, double* __restrict__ Scol, int ldsc,
+                          double* __restrict__ dsm) {
+    __syncthreads();
     double* b = dsm;               // s x nZ, ld SMAX (only s rows used)
     double* y = dsm + SMAX * nZ;   // s x s, ld SMAX
     for (int e = threadIdx.x; e < mZ * nZ; e += blockDim.x) {
@@ -123,18 +135,26 @@ scol_kernel(const double* __restrict__ G, int ldg, int mZ, int s, int nZ,
         int i = e % s, j = e / s;
         Scol[(mZ + i) + (i64)j * ldsc] = b[i + j * SMAX];
     }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(SM_THREADS)
+scol_kernel(const double* __restrict__ G, int ldg, int mZ, int s, int nZ,
+            const double* __restrict__ Yd, int ldy, double* __restrict__ Scol, int ldsc) {
+    extern __shared__ double dsm[];
+    scol_body(G, ldg, mZ, s, nZ, Yd, ldy, Scol, ldsc, dsm);
 }
 
 // R column block at columns [c0, c0+ny):
 //   mode 0: R[0:K, c0:] = A + B Sd ;  R[c0:c0+ny, c0:] = Yd Sd      (P1s, PIPI, BCGSI+, P2s)
 //   mode 1: R[0:K, c0:] = A + B    ;  upper(R[c0:c0+ny, c0:]) = upper(Yd)   (bcgsi21s)
 // A, B are K x ny (ld lda, ldb); Sd, Yd upper ny x ny.
-__global__ void __launch_bounds__(SM_THREADS)
-rblock_kernel(double* __restrict__ R, int ldR, int c0, int K, int ny,
-              const double* __restrict__ A, int lda, const double* __restrict__ B, int ldb,
-              const double* __restrict__ Sd, int ldsd, const double* __restrict__ Yd, int ldyd,
-              int mode) {
-    __shared__ double sd[SMAX * SMAX];
+// Body shared by the single and batched kernels; sd is SMAX*SMAX doubles.
+__device__ void rblock_body(double* __restrict__ R, int ldR, int c0, int K, int ny,
+                            const double* __restrict__ A, int lda, const double* __restrict__ B, int ldb,
+                            const double* __restrict__ Sd, int ldsd, const double* __restrict__ Yd, int ldyd,
+                            int mode, double* __restrict__ sd) {
+    __syncthreads();
     if (mode == 0) {
         for (int e = threadIdx.x; e < ny * ny; e += blockDim.x) {
             int i = e % ny, j = e / ny;
@@ -166,6 +186,16 @@ rblock_kernel(double* __restrict__ R, int ldR, int c0, int K, int ny,
             *dst = Yd[i + (i64)j * ldyd];
         }
     }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(SM_THREADS)
+rblock_kernel(double* __restrict__ R, int ldR, int c0, int K, int ny,
+              const double* __restrict__ A, int lda, const double* __restrict__ B, int ldb,
+              const double* __restrict__ Sd, int ldsd, const double* __restrict__ Yd, int ldyd,
+              int mode) {
+    __shared__ double sd[SMAX * SMAX];
+    rblock_body(R, ldR, c0, K, ny, A, lda, B, ldb, Sd, ldsd, Yd, ldyd, mode, sd);
 }
 
 int launch_pyth_chol(const double* Om, int ldom, const double* A, int lda, int k, int nz,
@@ -200,6 +230,30 @@ int launch_rblock(double* R, int ldR, int c0, int K, int ny, const double* A, in
     if (ny > SMAX) return (int)cudaErrorInvalidValue;
     rblock_kernel<<<1, SM_THREADS, 0, st>>>(R, ldR, c0, K, ny, A, lda, B, ldb, Sd, ldsd, Yd,
                                             ldyd, mode);
+    g_launch_count += 1;
+    return (int)cudaGetLastError();
+}
+
+// Batched form: one CTA per matrix runs that matrix's small operations of one stage
+// in order (each with the single-matrix body, so the arithmetic is the same).
+__global__ void __launch_bounds__(SM_THREADS)
+small_batched(const SmallJob* __restrict__ jobs) {
+    __shared__ double sm[SMAX * SMAX];
+    const SmallJob& J = jobs[blockIdx.x];
+    for (int q = 0; q < J.nsub; ++q) {
+        const SmallSub& S = J.sub[q];
+        if (S.kind == kSmallPyth)
+            pyth_chol_body(S.p0, S.ld0, S.p1, S.ld1, S.a, S.b, S.out, S.ldo, J.status, S.step, sm);
+        else if (S.kind == kSmallScol)
+            scol_body(S.p0, S.ld0, S.a, S.b, S.c, S.p1, S.ld1, S.out, S.ldo, sm);
+        else if (S.kind == kSmallRblock)
+            rblock_body(J.R, J.ldR, S.a, S.b, S.c, S.p0, S.ld0, S.p1, S.ld1, S.p2, S.ld2, S.p3, S.ld3, S.d, sm);
+    }
+}
+
+int launch_small_batched(const SmallJob* jobs, int njobs, cudaStream_t st) {
+    if (njobs <= 0) return 0;
+    small_batched<<<(unsigned)njobs, SM_THREADS, 0, st>>>(jobs);
     g_launch_count += 1;
     return (int)cudaGetLastError();
 }

@@ -12,65 +12,80 @@
 //       one fixed-order reduction.
 //   update_fp64 : Xc = (Xc - X[:, 0:K] S) T^{-1}, T upper triangular
 //       replaces dgemm('N','N') + dtrsm('R','U','N','N') (SRC/orth.c:173-176).
+#include "batched.h"
 #include "common.cuh"
 #include "kernels.h"
 
 namespace bcgs {
 
-// ---------------------------------------------------------------------------
-// Gram partials. CTA tile: 64 rows of C (columns of A) x 32 columns of C
-// (columns of B). 256 threads, each owning a 4 x 2 register tile. The CTA walks a
-// contiguous row range of X in sub-tiles of 32 rows staged in shared memory.
-// Partial sums go to part[chunk][i + j * na] (column-major na x nb per chunk).
-// ---------------------------------------------------------------------------
 namespace {
-constexpr int GT_A = 64;    // C rows per CTA
-constexpr int GT_B = 32;    // C columns per CTA
-constexpr int GT_R = 32;    // X rows per shared-memory sub-tile
+constexpr int GT_A = 64;    // C rows per CTA (single-matrix form)
+constexpr int GT_B = 32;    // C columns per CTA (single-matrix form)
+constexpr int GT_R = 32;    // chunk row ranges are multiples of this
 constexpr int GT_THREADS = 256;
 }  // namespace
 
-__global__ void __launch_bounds__(GT_THREADS)
-gram_fp64_partial(const double* __restrict__ X, i64 ld, i64 m, int a0, int na, int b0, int nb,
-                  i64 rows_per_chunk, double* __restrict__ part) {
-    __shared__ double sA[GT_R][GT_A + 1];
-    __shared__ double sB[GT_R][GT_B + 1];
-    const int chunk = blockIdx.x;
-    const int ia0 = blockIdx.y * GT_A;
-    const int jb0 = blockIdx.z * GT_B;
-    const i64 r_begin = (i64)chunk * rows_per_chunk;
-    const i64 r_end = min(m, r_begin + rows_per_chunk);
+// ---------------------------------------------------------------------------
+// Gram partials. CTA tile: GA = 2048/TB rows of C (columns of A) x TB columns of C
+// (columns of B), TB in {8, 16, 32}; 256 threads, each owning a 4 x 2 register
+// tile. The CTA walks a contiguous row range of X in sub-tiles of GR = TB rows
+// staged in shared memory. Partial sums go to part[chunk][i + j * na]
+// (column-major na x nb per chunk). Every entry is a sequential FMA chain over the
+// rows of the chunk in order, so the result does not depend on TB.
+// ---------------------------------------------------------------------------
+template <int TB>
+struct GramPanel {
+    static constexpr int GA = 2048 / TB;   // C rows per CTA
+    static constexpr int GR = TB;          // X rows per shared-memory sub-tile
+    static constexpr int SMEM = GR * (GA + 1) + GR * (TB + 1);   // doubles
+};
+constexpr int kGramSmemMax = GramPanel<32>::SMEM > GramPanel<8>::SMEM
+                                 ? (GramPanel<32>::SMEM > GramPanel<16>::SMEM ? GramPanel<32>::SMEM
+                                                                              : GramPanel<16>::SMEM)
+                                 : (GramPanel<8>::SMEM > GramPanel<16>::SMEM ? GramPanel<8>::SMEM
+                                                                             : GramPanel<16>::SMEM);
+
+// The tile at C rows ia0.., C columns jb0.., rows [r_begin, r_end) of X, written to
+// `out` (na x nb, ld na). 256 threads; sm holds GramPanel<TB>::SMEM doubles.
+template <int TB>
+__device__ __forceinline__ void gram_partial_body(const double* __restrict__ X, i64 ld, int a0, int na, int b0,
+                                                  int nb, i64 r_begin, i64 r_end, int ia0, int jb0,
+                                                  double* __restrict__ out, double* __restrict__ sm) {
+    constexpr int GA = GramPanel<TB>::GA, GR = GramPanel<TB>::GR, NT = 256;
+    constexpr int TI = GA / 4;      // threads along C rows -> 4 rows each
+    double (*sA)[GA + 1] = reinterpret_cast<double (*)[GA + 1]>(sm);
+    double (*sB)[TB + 1] = reinterpret_cast<double (*)[TB + 1]>(sm + GR * (GA + 1));
     const int tid = threadIdx.x;
-    const int ti = tid % 16;   // 16 threads along C rows  -> 4 rows each
-    const int tj = tid / 16;   // 16 threads along C cols  -> 2 cols each
+    const int ti = tid % TI;
+    const int tj = tid / TI;        // TB/2 threads along C cols -> 2 cols each
 
     double acc[4][2];
 #pragma unroll
     for (int a = 0; a < 4; ++a) { acc[a][0] = 0.0; acc[a][1] = 0.0; }
 
-    for (i64 r0 = r_begin; r0 < r_end; r0 += GT_R) {
-        // Stage A[r0:r0+32, ia0:ia0+64] and B[r0:r0+32, jb0:jb0+32]. Consecutive
-        // threads read consecutive rows of one column: coalesced 256-byte runs.
-        for (int e = tid; e < GT_R * GT_A; e += GT_THREADS) {
-            int rr = e % GT_R, cc = e / GT_R;
+    for (i64 r0 = r_begin; r0 < r_end; r0 += GR) {
+        // Stage A[r0:r0+GR, ia0:ia0+GA] and B[r0:r0+GR, jb0:jb0+TB]. Consecutive
+        // threads read consecutive rows of one column.
+        for (int e = tid; e < GR * GA; e += NT) {
+            int rr = e % GR, cc = e / GR;
             i64 r = r0 + rr;
             int c = ia0 + cc;
             sA[rr][cc] = (r < r_end && c < na) ? X[r + (i64)(a0 + c) * ld] : 0.0;
         }
-        for (int e = tid; e < GT_R * GT_B; e += GT_THREADS) {
-            int rr = e % GT_R, cc = e / GT_R;
+        for (int e = tid; e < GR * TB; e += NT) {
+            int rr = e % GR, cc = e / GR;
             i64 r = r0 + rr;
             int c = jb0 + cc;
             sB[rr][cc] = (r < r_end && c < nb) ? X[r + (i64)(b0 + c) * ld] : 0.0;
         }
         __syncthreads();
 #pragma unroll 4
-        for (int rr = 0; rr < GT_R; ++rr) {
+        for (int rr = 0; rr < GR; ++rr) {
             double av[4], bv[2];
 #pragma unroll
-            for (int a = 0; a < 4; ++a) av[a] = sA[rr][ti + 16 * a];
+            for (int a = 0; a < 4; ++a) av[a] = sA[rr][ti + TI * a];
             bv[0] = sB[rr][tj];
-            bv[1] = sB[rr][tj + 16];
+            bv[1] = sB[rr][tj + TB / 2];
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 acc[a][0] = fma(av[a], bv[0], acc[a][0]);
@@ -79,16 +94,26 @@ gram_fp64_partial(const double* __restrict__ X, i64 ld, i64 m, int a0, int na, i
         }
         __syncthreads();
     }
-    double* out = part + (i64)chunk * na * nb;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-        int i = ia0 + ti + 16 * a;
+        int i = ia0 + ti + TI * a;
 #pragma unroll
         for (int b = 0; b < 2; ++b) {
-            int j = jb0 + tj + 16 * b;
+            int j = jb0 + tj + (TB / 2) * b;
             if (i < na && j < nb) out[i + (i64)j * na] = acc[a][b];
         }
     }
+}
+
+__global__ void __launch_bounds__(GT_THREADS, 4)
+gram_fp64_partial(const double* __restrict__ X, i64 ld, i64 m, int a0, int na, int b0, int nb,
+                  i64 rows_per_chunk, double* __restrict__ part) {
+    __shared__ double sm[GramPanel<GT_B>::SMEM];
+    const int chunk = blockIdx.x;
+    const i64 r_begin = (i64)chunk * rows_per_chunk;
+    const i64 r_end = min(m, r_begin + rows_per_chunk);
+    gram_partial_body<GT_B>(X, ld, a0, na, b0, nb, r_begin, r_end, blockIdx.y * GT_A, blockIdx.z * GT_B,
+                            part + (i64)chunk * na * nb, sm);
 }
 
 // Fixed-order sum over chunks: out[i + j*ldo] = sum_{c=0}^{nchunks-1} part[c][i + j*na].
@@ -106,7 +131,15 @@ __global__ void gram_reduce(const double* __restrict__ part, int nchunks, int na
     }
 }
 
+// Rows per Gram chunk forced by orth_gb300_set_gram_chunk_rows (0: the default
+// policy below).
+long long g_gram_chunk_rows = 0;
+
 int gram_chunks_fp64(i64 m, int na, int nb, int num_sms) {
+    if (g_gram_chunk_rows > 0) {
+        const i64 c = ceil_div(m, g_gram_chunk_rows);
+        return (int)(c < 1 ? 1 : c);
+    }
     const i64 tiles = ceil_div(na, GT_A) * ceil_div(nb, GT_B);
     // About four CTAs per SM in total, each with at least 256 rows.
     i64 want = ceil_div(4LL * num_sms, tiles);
@@ -157,16 +190,23 @@ constexpr int UP_THREADS = 128;
 template <int NC>
 struct UpChunk { static constexpr int value = NC <= 16 ? 64 : (NC <= 32 ? 32 : 16); };
 
+// Shared-memory doubles update_body<NC> needs: S chunk, T, T's reciprocal diagonal.
 template <int NC>
-__global__ void __launch_bounds__(UP_THREADS)
-update_fp64(double* __restrict__ X, i64 ld, i64 m, int q0, int K, int c0, int nc,
-            const double* __restrict__ S, int lds, const double* __restrict__ T, int ldt) {
+struct UpSmem { static constexpr int value = UpChunk<NC>::value * NC + NC * NC + NC; };
+
+// Rows [r0, r0 + 128) of the update, one row per thread (128 threads). sm holds
+// UpSmem<NC>::value doubles. Every output is an FMA chain over k in order, then the
+// forward substitution in column order, so the result does not depend on NC >= nc.
+template <int NC>
+__device__ __forceinline__ void update_body(double* __restrict__ X, i64 ld, i64 m, int q0, int K, int c0, int nc,
+                                            const double* __restrict__ S, int lds, const double* __restrict__ T,
+                                            int ldt, i64 r0, double* __restrict__ sm) {
     constexpr int KCH = UpChunk<NC>::value;
-    __shared__ double sS[KCH][NC];
-    __shared__ double sT[NC][NC];
-    __shared__ double sRd[NC];
+    double (*sS)[NC] = reinterpret_cast<double (*)[NC]>(sm);
+    double (*sT)[NC] = reinterpret_cast<double (*)[NC]>(sm + KCH * NC);
+    double* sRd = sm + KCH * NC + NC * NC;
     const int tid = threadIdx.x;
-    const i64 r = blockIdx.x * (i64)UP_THREADS + tid;
+    const i64 r = r0 + tid;
     if (T != nullptr) {
         for (int e = tid; e < NC * NC; e += UP_THREADS) {
             int i = e % NC, j = e / NC;
@@ -199,31 +239,43 @@ update_fp64(double* __restrict__ X, i64 ld, i64 m, int q0, int K, int c0, int nc
         }
     }
     __syncthreads();
-    if (!live) return;
-    double* xr = X + r + (i64)c0 * ld;
-    // acc becomes w = x - Q S in place.
+    if (live) {
+        double* xr = X + r + (i64)c0 * ld;
+        // acc becomes w = x - Q S in place.
 #pragma unroll
-    for (int j = 0; j < NC; ++j) acc[j] = (j < nc) ? xr[(i64)j * ld] - acc[j] : 0.0;
-    if (T != nullptr) {
-        // Forward substitution u T = w (dtrsm 'R','U','N','N'), column by column.
+        for (int j = 0; j < NC; ++j) acc[j] = (j < nc) ? xr[(i64)j * ld] - acc[j] : 0.0;
+        if (T != nullptr) {
+            // Forward substitution u T = w (dtrsm 'R','U','N','N'), column by column.
 #pragma unroll
-        for (int j = 0; j < NC; ++j) {
-            double v = acc[j];
+            for (int j = 0; j < NC; ++j) {
+                double v = acc[j];
 #pragma unroll
-            for (int i = 0; i < j; ++i) v = fma(-acc[i], sT[i][j], v);
-            acc[j] = v * sRd[j];
+                for (int i = 0; i < j; ++i) v = fma(-acc[i], sT[i][j], v);
+                acc[j] = v * sRd[j];
+            }
         }
-    }
 #pragma unroll
-    for (int j = 0; j < NC; ++j)
-        if (j < nc) xr[(i64)j * ld] = acc[j];
+        for (int j = 0; j < NC; ++j)
+            if (j < nc) xr[(i64)j * ld] = acc[j];
+    }
+    __syncthreads();   // sm is reused by the caller's next tile
+}
+
+template <int NC>
+__global__ void __launch_bounds__(UP_THREADS)
+update_fp64(double* __restrict__ X, i64 ld, i64 m, int q0, int K, int c0, int nc,
+            const double* __restrict__ S, int lds, const double* __restrict__ T, int ldt) {
+    __shared__ double sm[UpSmem<NC>::value];
+    update_body<NC>(X, ld, m, q0, K, c0, nc, S, lds, T, ldt, blockIdx.x * (i64)UP_THREADS, sm);
 }
 
 int launch_update_fp64(double* X, i64 ld, i64 m, int q0, int K, int c0, int nc,
                        const double* S, int lds, const double* T, int ldt, cudaStream_t st) {
     if (nc <= 0 || m <= 0) return 0;
     dim3 grid((unsigned)ceil_div(m, UP_THREADS));
-    if (nc <= 8)
+    if (nc <= 4)
+        update_fp64<4><<<grid, UP_THREADS, 0, st>>>(X, ld, m, q0, K, c0, nc, S, lds, T, ldt);
+    else if (nc <= 8)
         update_fp64<8><<<grid, UP_THREADS, 0, st>>>(X, ld, m, q0, K, c0, nc, S, lds, T, ldt);
     else if (nc <= 16)
         update_fp64<16><<<grid, UP_THREADS, 0, st>>>(X, ld, m, q0, K, c0, nc, S, lds, T, ldt);
@@ -233,6 +285,82 @@ int launch_update_fp64(double* X, i64 ld, i64 m, int q0, int K, int c0, int nc,
         update_fp64<64><<<grid, UP_THREADS, 0, st>>>(X, ld, m, q0, K, c0, nc, S, lds, T, ldt);
     else
         return (int)cudaErrorInvalidValue;
+    g_launch_count += 1;
+    return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Batched forms: one launch over many matrices' jobs (batched.h).
+// ---------------------------------------------------------------------------
+int gram_batched_panel_rows(int tb) { return 2048 / tb; }
+
+__global__ void __launch_bounds__(GT_THREADS, 4)
+gram_partial_batched(const GramJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
+    __shared__ double sm[kGramSmemMax];
+    const int j = batched_job_of(prefix, njobs, blockIdx.x);
+    const GramJob& J = jobs[j];
+    const int local = blockIdx.x - prefix[j];
+    const int chunk = local % J.nchunks;
+    const int t = local / J.nchunks;
+    const int ia = t % J.tilesA, jb = t / J.tilesA;
+    const i64 r_begin = (i64)chunk * J.rows_per_chunk;
+    const i64 r_end = min(J.m, r_begin + J.rows_per_chunk);
+    double* out = J.part + (i64)chunk * J.na * J.nb;
+    if (J.tb == 8)
+        gram_partial_body<8>(J.X, J.ld, 0, J.na, J.b0, J.nb, r_begin, r_end, ia * GramPanel<8>::GA, jb * 8, out, sm);
+    else if (J.tb == 16)
+        gram_partial_body<16>(J.X, J.ld, 0, J.na, J.b0, J.nb, r_begin, r_end, ia * GramPanel<16>::GA, jb * 16, out,
+                              sm);
+    else
+        gram_partial_body<32>(J.X, J.ld, 0, J.na, J.b0, J.nb, r_begin, r_end, ia * GramPanel<32>::GA, jb * 32, out,
+                              sm);
+}
+
+// Same summation order as gram_reduce: each entry sums the chunks in order.
+__global__ void __launch_bounds__(256)
+gram_reduce_batched(const GramJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
+    const int j = batched_job_of(prefix, njobs, blockIdx.x);
+    const GramJob& J = jobs[j];
+    const i64 total = (i64)J.na * J.nb;
+    const i64 e = (i64)(blockIdx.x - prefix[j]) * 256 + threadIdx.x;
+    if (e >= total) return;
+    double s = 0.0;
+    for (int c = 0; c < J.nchunks; ++c) s += J.part[(i64)c * total + e];
+    const int i = (int)(e % J.na), jj = (int)(e / J.na);
+    J.C[i + (i64)jj * J.ldc] = s;
+}
+
+__global__ void __launch_bounds__(UP_THREADS)
+update_batched(const UpdJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
+    __shared__ double sm[UpSmem<16>::value];
+    const int j = batched_job_of(prefix, njobs, blockIdx.x);
+    const UpdJob& J = jobs[j];
+    const i64 r0 = (i64)(blockIdx.x - prefix[j]) * UP_THREADS;
+    if (J.nc <= 4)
+        update_body<4>(J.X, J.ld, J.m, J.q0, J.K, J.c0, J.nc, J.S, J.lds, J.T, J.ldt, r0, sm);
+    else if (J.nc <= 8)
+        update_body<8>(J.X, J.ld, J.m, J.q0, J.K, J.c0, J.nc, J.S, J.lds, J.T, J.ldt, r0, sm);
+    else
+        update_body<16>(J.X, J.ld, J.m, J.q0, J.K, J.c0, J.nc, J.S, J.lds, J.T, J.ldt, r0, sm);
+}
+
+int launch_gram_partial_batched(const GramJob* jobs, const int* prefix, int njobs, int items, cudaStream_t st) {
+    if (items <= 0) return 0;
+    gram_partial_batched<<<(unsigned)items, GT_THREADS, 0, st>>>(jobs, prefix, njobs);
+    g_launch_count += 1;
+    return (int)cudaGetLastError();
+}
+
+int launch_gram_reduce_batched(const GramJob* jobs, const int* prefix, int njobs, int items, cudaStream_t st) {
+    if (items <= 0) return 0;
+    gram_reduce_batched<<<(unsigned)items, 256, 0, st>>>(jobs, prefix, njobs);
+    g_launch_count += 1;
+    return (int)cudaGetLastError();
+}
+
+int launch_update_batched(const UpdJob* jobs, const int* prefix, int njobs, int items, cudaStream_t st) {
+    if (items <= 0) return 0;
+    update_batched<<<(unsigned)items, UP_THREADS, 0, st>>>(jobs, prefix, njobs);
     g_launch_count += 1;
     return (int)cudaGetLastError();
 }

@@ -15,6 +15,7 @@
 //
 // Every reduction is in a fixed order (block reductions with a fixed warp order,
 // a fixed tree), so results are bit-identical run to run.
+#include "batched.h"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -52,11 +53,11 @@ __device__ __forceinline__ void block_sum_vec(const double* v, int cnt, double* 
 // Writes the explicit tile Q (same rows) to Q (ldq; may alias A) and the tile R to
 // Rst rows [t*nc, (t+1)*nc) (ld ldr), lower part zero. Tiles shorter than nc rows
 // are padded with zero rows (their padded Q rows are not written).
+// Body shared by the single and batched kernels: tile `tile` of the level matrix;
+// smem holds tsqr_tile_smem_doubles(TR, NC) doubles.
 template <int NC>
-__global__ void __launch_bounds__(256)
-tsqr_tile_kernel(const double* A, i64 lda, i64 rows, int nc, double* Q, i64 ldq,
-                 double* __restrict__ Rst, i64 ldr) {
-    extern __shared__ double smem[];
+__device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, double* Q, i64 ldq,
+                               double* __restrict__ Rst, i64 ldr, i64 tile, double* smem) {
     const int TR = blockDim.x;
     const int TRP = TR + 1;
     double* a = smem;                       // TR x NC, column-major, ld TRP
@@ -67,7 +68,8 @@ tsqr_tile_kernel(const double* A, i64 lda, i64 rows, int nc, double* Q, i64 ldq,
     __shared__ double s_sc[2];
 
     const int r = threadIdx.x;
-    const i64 row0 = (i64)blockIdx.x * TR;
+    __syncthreads();
+    const i64 row0 = tile * TR;
     const i64 h = min((i64)TR, rows - row0);
     for (int c = 0; c < NC; ++c)
         a[r + c * TRP] = (c < nc && r < h) ? A[row0 + r + (i64)c * lda] : 0.0;
@@ -116,7 +118,7 @@ tsqr_tile_kernel(const double* A, i64 lda, i64 rows, int nc, double* Q, i64 ldq,
     // R to the stack (upper, lower zero).
     for (int e = r; e < nc * nc; e += TR) {
         int i = e % nc, c = e / nc;
-        Rst[(i64)blockIdx.x * nc + i + (i64)c * ldr] = (i <= c) ? a[i + c * TRP] : 0.0;
+        Rst[tile * nc + i + (i64)c * ldr] = (i <= c) ? a[i + c * TRP] : 0.0;
     }
     // Explicit Q = H_0 ... H_{nc-1} [I; 0] (dorg2r), backward accumulation.
     for (int c = 0; c < NC; ++c) q[r + c * TRP] = (c < nc && r == c) ? 1.0 : 0.0;
@@ -136,14 +138,24 @@ tsqr_tile_kernel(const double* A, i64 lda, i64 rows, int nc, double* Q, i64 ldq,
     }
     if (r < h)
         for (int c = 0; c < nc; ++c) Q[row0 + r + (i64)c * ldq] = q[r + c * TRP];
+    __syncthreads();
+}
+
+template <int NC>
+__global__ void __launch_bounds__(256)
+tsqr_tile_kernel(const double* A, i64 lda, i64 rows, int nc, double* Q, i64 ldq,
+                 double* __restrict__ Rst, i64 ldr) {
+    extern __shared__ double smem[];
+    tsqr_tile_body<NC>(A, lda, rows, nc, Q, ldq, Rst, ldr, blockIdx.x, smem);
 }
 
 // Root fix-up: make diag(R) >= 0. R (nc x nc, ld ldr) rows with a negative
 // diagonal are negated, as are the matching columns of the root Q (hq x nc, ldq).
 // The final R is also copied to Rout (ld ldro), lower part zero.
-__global__ void tsqr_root_fix(double* Q, i64 ldq, int hq, int nc, const double* R, i64 ldr,
-                              double* Rout, int ldro) {
+__device__ void tsqr_root_fix_body(double* Q, i64 ldq, int hq, int nc, const double* R, i64 ldr,
+                                   double* Rout, int ldro) {
     __shared__ double sgn[64];
+    __syncthreads();
     if (threadIdx.x < nc) sgn[threadIdx.x] = (R[threadIdx.x + (i64)threadIdx.x * ldr] < 0.0) ? -1.0 : 1.0;
     __syncthreads();
     for (int e = threadIdx.x; e < nc * nc; e += blockDim.x) {
@@ -154,22 +166,30 @@ __global__ void tsqr_root_fix(double* Q, i64 ldq, int hq, int nc, const double* 
         int i = e % hq, c = e / hq;
         Q[i + (i64)c * ldq] *= sgn[c];
     }
+    __syncthreads();
+}
+
+__global__ void tsqr_root_fix(double* Q, i64 ldq, int hq, int nc, const double* R, i64 ldr,
+                              double* Rout, int ldro) {
+    tsqr_root_fix_body(Q, ldq, hq, nc, R, ldr, Rout, ldro);
 }
 
 // Down-sweep: for each tile t of TR rows of Q (rows x nc, ldq):
 //   Q[tile t] = Q[tile t] * P[t*nc:(t+1)*nc, 0:nc]   (P: ld ldp)
+// Body shared by the single and batched kernels: rows [blk*blockDim, ...) of Q.
 template <int NC>
-__global__ void __launch_bounds__(256)
-tsqr_apply_kernel(double* Q, i64 ldq, i64 rows, int nc, int TR, const double* __restrict__ P, i64 ldp) {
+__device__ void tsqr_apply_body(double* Q, i64 ldq, i64 rows, int nc, int TR, const double* __restrict__ P,
+                                i64 ldp, i64 blk) {
     __shared__ double p[NC * NC];
-    const i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    const i64 t = ((i64)blockIdx.x * blockDim.x) / TR;   // blockDim.x divides TR
+    __syncthreads();
+    const i64 r = blk * blockDim.x + threadIdx.x;
+    const i64 t = (blk * blockDim.x) / TR;   // blockDim.x divides TR
     for (int e = threadIdx.x; e < nc * nc; e += blockDim.x) {
         int i = e % nc, c = e / nc;
         p[i + c * NC] = P[t * nc + i + (i64)c * ldp];
     }
     __syncthreads();
-    if (r >= rows) return;
+    if (r >= rows) return;   // the last statement of the body: no barrier follows
     double x[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) x[c] = (c < nc) ? Q[r + (i64)c * ldq] : 0.0;
@@ -181,6 +201,12 @@ tsqr_apply_kernel(double* Q, i64 ldq, i64 rows, int nc, int TR, const double* __
         for (int i = 0; i < NC; ++i) y = fma(x[i], p[i + c * NC], y);
         Q[r + (i64)c * ldq] = y;
     }
+}
+
+template <int NC>
+__global__ void __launch_bounds__(256)
+tsqr_apply_kernel(double* Q, i64 ldq, i64 rows, int nc, int TR, const double* __restrict__ P, i64 ldp) {
+    tsqr_apply_body<NC>(Q, ldq, rows, nc, TR, P, ldp, blockIdx.x);
 }
 
 i64 tsqr_workspace_doubles(i64 m, int nc) {
@@ -251,6 +277,75 @@ int launch_tsqr(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR, do
     if (nc <= 32) return tsqr_run<32>(X, ld, m, c0, nc, R, ldR, ws, st);
     if (nc <= 64) return tsqr_run<64>(X, ld, m, c0, nc, R, ldR, ws, st);
     return (int)cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
+// Batched forms (batched.h): tiles of one tree level, root sign fixes and one
+// down-sweep level over many panels (nc <= 16, TR = 256), with the single-panel
+// bodies.
+// ---------------------------------------------------------------------------
+static size_t tsqr_tile_smem_bytes(int TR, int NC) {
+    return (size_t)(2 * (TR + 1) * NC + TQ_MAXW * NC + 2 * NC) * sizeof(double);
+}
+
+__global__ void __launch_bounds__(256)
+tsqr_tile_batched(const TsqrTileJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
+    extern __shared__ double smem[];
+    const int j = batched_job_of(prefix, njobs, blockIdx.x);
+    const TsqrTileJob& J = jobs[j];
+    const i64 tile = blockIdx.x - prefix[j];
+    if (J.nc <= 8)
+        tsqr_tile_body<8>(J.A, J.lda, J.rows, J.nc, J.A, J.lda, J.Rst, J.ldr, tile, smem);
+    else
+        tsqr_tile_body<16>(J.A, J.lda, J.rows, J.nc, J.A, J.lda, J.Rst, J.ldr, tile, smem);
+}
+
+__global__ void tsqr_root_batched(const TsqrRootJob* __restrict__ jobs) {
+    const TsqrRootJob& J = jobs[blockIdx.x];
+    tsqr_root_fix_body(J.Q, J.ldq, J.hq, J.nc, J.R, J.ldr, J.Rout, J.ldro);
+}
+
+__global__ void __launch_bounds__(128)
+tsqr_apply_batched(const TsqrApplyJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
+    const int j = batched_job_of(prefix, njobs, blockIdx.x);
+    const TsqrApplyJob& J = jobs[j];
+    const i64 blk = blockIdx.x - prefix[j];
+    if (J.nc <= 8)
+        tsqr_apply_body<8>(J.Q, J.ldq, J.rows, J.nc, J.TR, J.P, J.ldp, blk);
+    else
+        tsqr_apply_body<16>(J.Q, J.ldq, J.rows, J.nc, J.TR, J.P, J.ldp, blk);
+}
+
+// Sets the batched tile kernel's shared-memory limit (outside any stream capture).
+int tsqr_tile_batched_prepare() {
+    return (int)cudaFuncSetAttribute(tsqr_tile_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tsqr_tile_smem_bytes(256, 16));
+}
+
+int launch_tsqr_tile_batched(const TsqrTileJob* jobs, const int* prefix, int njobs, int items, int ncmax,
+                             cudaStream_t st) {
+    if (items <= 0) return 0;
+    if (ncmax > 16) return (int)cudaErrorInvalidValue;
+    const size_t smem = tsqr_tile_smem_bytes(256, 16);
+    tsqr_tile_batched<<<(unsigned)items, 256, smem, st>>>(jobs, prefix, njobs);
+    g_launch_count += 1;
+    return (int)cudaGetLastError();
+}
+
+int launch_tsqr_root_batched(const TsqrRootJob* jobs, int njobs, cudaStream_t st) {
+    if (njobs <= 0) return 0;
+    tsqr_root_batched<<<(unsigned)njobs, 256, 0, st>>>(jobs);
+    g_launch_count += 1;
+    return (int)cudaGetLastError();
+}
+
+int launch_tsqr_apply_batched(const TsqrApplyJob* jobs, const int* prefix, int njobs, int items, int ncmax,
+                              cudaStream_t st) {
+    if (items <= 0) return 0;
+    if (ncmax > 16) return (int)cudaErrorInvalidValue;
+    tsqr_apply_batched<<<(unsigned)items, 128, 0, st>>>(jobs, prefix, njobs);
+    g_launch_count += 1;
+    return (int)cudaGetLastError();
 }
 
 }  // namespace bcgs

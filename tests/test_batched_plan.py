@@ -1,0 +1,64 @@
+"""CPU tests of the batched plan's schedule (orth_gb300_batch_dry_run).
+
+The batched form lays each matrix's BCGSI+P-1S steps (SRC/orth.c:48-222) on a
+common stage sequence: the TSQR tree of block 1 (one stage per level, the root
+sign fixes, one per down-sweep level), the first step's six stages, and four per
+later block step. A Gram stage is two launches (partials, fixed-order reduction).
+"""
+import numpy as np
+import pytest
+
+from bcgs_gb300 import orth
+
+
+def _tsqr_levels(m, tr=256, s=8):
+    levels, rows = 0, m
+    while rows > tr:
+        rows = -(-rows // tr) * s
+        levels += 1
+    return levels
+
+
+def _expected(ms, ns, ss):
+    L = max(_tsqr_levels(m, s=s) for m, s in zip(ms, ss))
+    p = max((n - s + s - 1) // s for n, s in zip(ns, ss))
+    stages = (L + 1) + 1 + L + 6 + 4 * (p - 1)
+    grams = 2 + (p - 1)
+    return stages, stages + grams
+
+
+@pytest.mark.parametrize("case", [
+    ([3000], [32], [8]),
+    ([3000, 200000, 5000], [32, 256, 8], [8, 16, 4]),
+    ([2000] * 5, [8, 16, 24, 32, 40], [4, 4, 4, 4, 4]),
+])
+def test_dry_run_stage_counts(lib, case):
+    ms, ns, ss = case
+    d = orth.batch_dry_run(ms, ns, ss)
+    assert d["rc"] == 0
+    assert (d["stages"], d["launches"]) == _expected(ms, ns, ss)
+    assert d["bytes"] > 0
+
+
+def test_dry_run_config4_size(lib):
+    rng = np.random.default_rng(2024)
+    B = 4096
+    m = np.exp(rng.uniform(np.log(2000), np.log(200000), B)).astype(int)
+    s = rng.choice([4, 8, 16], B)
+    p = rng.integers(2, 17, B)
+    d = orth.batch_dry_run(m.tolist(), (s * p).tolist(), s.tolist())
+    assert d["rc"] == 0
+    # 16 blocks at most: 15 block steps after the first; stays one graph of < 100 launches.
+    assert d["launches"] < 100
+    # Plan workspace is a small fraction of the batch's own 120 GB.
+    assert d["bytes"] < 4e9
+
+
+@pytest.mark.parametrize("bad", [
+    ([3000], [64], [32]),      # s > 16
+    ([3000], [12], [8]),       # n < 2s
+    ([10], [16], [8]),         # m < n
+    ([3000], [32], [0]),       # s < 1
+])
+def test_dry_run_rejects(lib, bad):
+    assert orth.batch_dry_run(*bad)["rc"] == 2
