@@ -59,7 +59,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
-    ap.add_argument("--workload", choices=["qr", "batched"], default="qr",
+    ap.add_argument("--kappas", default="1e2,1e6,1e10,1e14", help="sweep workload: condition numbers")
+    ap.add_argument("--monomial", action="store_true",
+                    help="sweep workload: add the s-step monomial basis (m=2^22, s=8, n=512)")
+    ap.add_argument("--workload", choices=["qr", "batched", "sweep"], default="qr",
                     help="qr: one BCGSI+P-1S QR of m x n (default); batched: the batched form "
                          "(--batch matrices of uneven m, s, p and kappa in one captured CUDA graph)")
     ap.add_argument("--batch", type=int, default=4096)
@@ -556,6 +559,70 @@ def run_batched(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def run_sweep(args, rank, world, local_rank):
+    """Accuracy and time per condition number (and for the monomial basis): the
+    variant in FP64 and both split-precision forms, with the library's metrics."""
+    import numpy as np
+    import torch
+
+    from bcgs_gb300 import inputs, orth
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    orth.load()
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    cases = [("graded", float(k), args.m, args.n, args.s) for k in args.kappas.split(",") if k]
+    if args.monomial:
+        cases.append(("monomial", None, 1 << 22, 512, 8))
+    rows = []
+    for kind, kappa, m, n, s in cases:
+        if kind == "graded":
+            X0 = inputs.graded_device(m, n, kappa, seed=1234, device=str(dev))
+        else:
+            X0 = inputs.monomial_device(m, n, s, seed=1234, device=str(dev))
+        X = torch.empty_like(X0)
+        R = torch.zeros((n, n), dtype=torch.float64, device=dev)
+        E = torch.empty((n, n), dtype=torch.float64, device=dev)
+        precs = [("fp64", orth.FP64)]
+        if orth.split_supported(m, n, s):
+            precs += [("split7", orth.SPLIT_BF16), ("split6", orth.SPLIT_BF16_FAST)]
+        for name, prec in precs:
+            times, st = [], None
+            for k in range(2):
+                with torch.cuda.stream(stream):
+                    X.copy_(X0)
+                    R.zero_()
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    rc, st = orth.run_dev(args.variant, m, n, s, X.data_ptr(), m, R.data_ptr(), n, prec, sptr)
+                    b.record(stream)
+                if rc != 0:
+                    raise RuntimeError(f"run_dev rc={rc}")
+                torch.cuda.synchronize()
+                if k > 0:
+                    times.append(a.elapsed_time(b))
+            gp = orth.SPLIT_BF16 if orth.split_supported(m, n, 16) else orth.FP64
+            rc, loo_f, res_f, x_f = orth.accuracy_dev(m, n, X0.data_ptr(), m, X.data_ptr(), m, R.data_ptr(), n, gp,
+                                                      E.data_ptr(), n, sptr)
+            if rc != 0:
+                raise RuntimeError(f"accuracy_dev rc={rc}")
+            Eh = E.cpu().numpy()
+            finite = bool(np.isfinite(Eh).all())
+            rows.append({"input": kind, "kappa": kappa, "m": m, "n": n, "s": s, "precision": name,
+                         "ms": round(times[0], 3),
+                         "loo_2": float(np.max(np.abs(np.linalg.eigvalsh(Eh)))) if finite else None,
+                         "loo_fro": loo_f, "rel_residual": res_f / x_f if x_f > 0 else 0.0,
+                         "breakdown_step": st["breakdown_step"], "breakdown_info": st["breakdown_info"]})
+            print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+        del X0, X
+        torch.cuda.empty_cache()
+    if rank == 0:
+        print(json.dumps({"metric": "accuracy and ms per QR across condition numbers", "variant": args.variant,
+                          "workload": "sweep", "metrics": "orth_gb300_accuracy_dev (exact digit Gram)",
+                          "rows": rows}), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local_rank = dist_env()
@@ -568,6 +635,8 @@ def main():
     try:
         if args.workload == "batched":
             run_batched(args, rank, world, local_rank)
+        elif args.workload == "sweep":
+            run_sweep(args, rank, world, local_rank)
         else:
             run_ours(args, rank, world, local_rank)
     finally:
