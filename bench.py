@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--kappas", default="1e2,1e6,1e10,1e14", help="sweep workload: condition numbers")
+    ap.add_argument("--precisions", default="fp64,split7,split6", help="sweep workload: forms to run")
     ap.add_argument("--monomial", action="store_true",
                     help="sweep workload: add the s-step monomial basis (m=2^22, s=8, n=512)")
     ap.add_argument("--workload", choices=["qr", "batched", "sweep"], default="qr",
@@ -587,6 +588,7 @@ def run_sweep(args, rank, world, local_rank):
         precs = [("fp64", orth.FP64)]
         if orth.split_supported(m, n, s):
             precs += [("split7", orth.SPLIT_BF16), ("split6", orth.SPLIT_BF16_FAST)]
+        precs = [pr for pr in precs if pr[0] in args.precisions.split(",")]
         for name, prec in precs:
             times, st = [], None
             for k in range(2):

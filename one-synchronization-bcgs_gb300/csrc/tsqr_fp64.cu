@@ -4,145 +4,171 @@
 // call sites :107,:271,:413,:505,:522,:534,:601,:613,:651). Trilinos is not part of
 // the reference, so the algorithm here is the published TSQR reduction tree:
 //
-//   level 0: the panel is cut into tiles of TR rows; each CTA computes a
-//            Householder QR of its tile in shared memory, writes the explicit tile
-//            Q in place and its nc x nc R into the next level's stack.
+//   level 0: the panel is cut into tiles of TR rows; one warp per tile computes a
+//            Householder QR of its tile in shared memory (warp butterfly sums, no
+//            block barriers), writes the explicit tile Q in place and its nc x nc
+//            R into the next level's stack.
 //   level l: the stacked R factors (a (tiles * nc) x nc matrix) are cut into tiles
 //            of TR rows again and factored the same way, until one tile remains.
 //   root   : R is sign-normalized (diag(R) >= 0, the column signs moved into Q).
 //   down   : each level's tile Q is multiplied by its nc x nc block of the level
 //            above, from the root down to the panel, giving the explicit Q.
 //
-// Every reduction is in a fixed order (block reductions with a fixed warp order,
-// a fixed tree), so results are bit-identical run to run.
+// Every reduction is in a fixed order (warp butterfly sums, a fixed tree), so
+// results are bit-identical run to run.
 #include "batched.h"
 #include "common.cuh"
 #include "kernels.h"
 
 namespace bcgs {
 
-namespace {
-constexpr int TQ_MAXW = 8;  // warps in the reduction scratch (TR <= 256)
-}
-
 int tsqr_tile_rows(int nc) { return nc <= 32 ? 256 : 128; }
 
-// Block-wide sum of `cnt` per-thread values in v[0..cnt), fixed order. Result in
-// out[0..cnt) (shared). Requires blockDim.x == TR (multiple of 32, <= 256).
-template <int MAXC>
-__device__ __forceinline__ void block_sum_vec(const double* v, int cnt, double* red, double* out) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+// Shared memory of one tile: the TR x NC tile, column-major (ld TR), and its NC
+// Householder scalars.
+static size_t tsqr_tile_smem_bytes(int TR, int NC) { return (size_t)(TR * NC + NC) * sizeof(double); }
+
+// Sums of G values over the warp by an xor butterfly. Lane pairs add the same two
+// operands (a + b == b + a), so every lane ends with the same bits, in a fixed order.
+template <int G>
+__device__ __forceinline__ void warp_sum(double* w) {
 #pragma unroll
-    for (int c = 0; c < MAXC; ++c) {
-        if (c >= cnt) break;
-        double x = v[c];
+    for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-        if (lane == 0) red[warp * MAXC + c] = x;
+        for (int g = 0; g < G; ++g) w[g] += __shfl_xor_sync(0xffffffffu, w[g], o);
     }
-    __syncthreads();
-    for (int c = threadIdx.x; c < cnt; c += blockDim.x) {
-        double s = 0.0;
-        for (int w = 0; w < nwarps; ++w) s += red[w * MAXC + c];
-        out[c] = s;
-    }
-    __syncthreads();
 }
 
-// One CTA per tile. A: rows x nc (lda); tile t covers rows [t*TR, min(rows,(t+1)*TR)).
-// Writes the explicit tile Q (same rows) to Q (ldq; may alias A) and the tile R to
-// Rst rows [t*nc, (t+1)*nc) (ld ldr), lower part zero. Tiles shorter than nc rows
-// are padded with zero rows (their padded Q rows are not written).
-// Body shared by the single and batched kernels: tile `tile` of the level matrix;
-// smem holds tsqr_tile_smem_doubles(TR, NC) doubles.
+// w_c = sum over the tile's rows of v[r] * a[r][c] for G columns c0.., then
+// a[r][c] -= (t w_c) v[r]. Lane `lane` owns rows lane + 32 i (i < RPL); v is zero
+// above the reflector's pivot row, so those rows are left as they are.
+template <int RPL, int G>
+__device__ __forceinline__ void apply_reflector(double* a, int TR, int c0, const double* v, double t, int lane) {
+    double w[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        w[g] = 0.0;
+#pragma unroll
+        for (int i = 0; i < RPL; ++i) w[g] = fma(v[i], a[(c0 + g) * TR + lane + 32 * i], w[g]);
+    }
+    warp_sum<G>(w);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        const double tw = t * w[g];
+#pragma unroll
+        for (int i = 0; i < RPL; ++i) {
+            double* e = &a[(c0 + g) * TR + lane + 32 * i];
+            *e = fma(-tw, v[i], *e);
+        }
+    }
+}
+
+// One warp per tile, the tile in shared memory (lane L owns rows L, L+32, ...).
+// A: rows x nc (lda); tile `tile` covers rows [tile*TR, min(rows, (tile+1)*TR)).
+// Householder QR by the conventions of LAPACK's dgeqr2/dlarfg (column j:
+// beta = -sign(alpha) sqrt(alpha^2 + ||x||^2), tau = (beta - alpha)/beta,
+// v = x / (alpha - beta)), then the tile's R (upper, lower part zero) to Rst rows
+// [tile*nc, (tile+1)*nc) (ld ldr), then the explicit tile Q formed in place in
+// dorg2r's order (backward over the reflectors) and written to Q (ldq; may alias
+// A). Tiles shorter than nc rows are padded with zero rows; padded rows of Q are
+// not written. Every dot product is a warp butterfly sum, so the result is
+// bit-identical run to run. smem holds tsqr_tile_smem_bytes(TR, NC).
 template <int NC>
 __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, double* Q, i64 ldq,
                                double* __restrict__ Rst, i64 ldr, i64 tile, double* smem) {
-    const int TR = blockDim.x;
-    const int TRP = TR + 1;
-    double* a = smem;                       // TR x NC, column-major, ld TRP
-    double* q = a + (size_t)TRP * NC;       // TR x NC
-    double* red = q + (size_t)TRP * NC;     // TQ_MAXW x NC
-    double* wv = red + TQ_MAXW * NC;        // NC
-    double* tau = wv + NC;                  // NC
-    __shared__ double s_sc[2];
-
-    const int r = threadIdx.x;
-    __syncthreads();
+    constexpr int TR = NC <= 32 ? 256 : 128;
+    constexpr int RPL = TR / 32;
+    double* a = smem;              // a[c * TR + r]
+    double* tau = smem + TR * NC;
+    const int lane = threadIdx.x & 31;
     const i64 row0 = tile * TR;
     const i64 h = min((i64)TR, rows - row0);
-    for (int c = 0; c < NC; ++c)
-        a[r + c * TRP] = (c < nc && r < h) ? A[row0 + r + (i64)c * lda] : 0.0;
-    __syncthreads();
-
-    double part[NC];
-    // Householder QR, LAPACK dgeqr2 / dlarfg conventions.
-    for (int j = 0; j < nc; ++j) {
-        double x = (r > j) ? a[r + j * TRP] : 0.0;
-        part[0] = x * x;
-        block_sum_vec<1>(part, 1, red, wv);
-        const double xnorm2 = wv[0];
-        if (r == 0) {
-            const double alpha = a[j + j * TRP];
-            double t = 0.0, beta = alpha, scal = 0.0;
-            if (xnorm2 > 0.0) {
-                beta = -copysign(sqrt(alpha * alpha + xnorm2), alpha);
-                t = (beta - alpha) / beta;
-                scal = 1.0 / (alpha - beta);
-            }
-            tau[j] = t;
-            s_sc[0] = beta;
-            s_sc[1] = scal;
-        }
-        __syncthreads();
-        const double beta = s_sc[0], scal = s_sc[1], tj = tau[j];
-        double v = 0.0;
-        if (r == j) v = 1.0;
-        else if (r > j) v = a[r + j * TRP] * scal;
-        __syncthreads();
-        if (r > j) a[r + j * TRP] = v;
-        if (r == j) a[j + j * TRP] = beta;
-        // Apply H_j = I - tau v v^T to columns j+1..nc-1.
-        const int cnt = nc - j - 1;
-        if (cnt > 0 && tj != 0.0) {
+    __syncwarp();
+    for (int c = 0; c < nc; ++c)
 #pragma unroll
-            for (int c = 0; c < NC; ++c)
-                if (c < cnt) part[c] = (r >= j) ? v * a[r + (j + 1 + c) * TRP] : 0.0;
-            block_sum_vec<NC>(part, cnt, red, wv);
-            if (r >= j) {
-                for (int c = 0; c < cnt; ++c) a[r + (j + 1 + c) * TRP] -= tj * wv[c] * v;
-            }
+        for (int i = 0; i < RPL; ++i) {
+            const int r = lane + 32 * i;
+            a[c * TR + r] = (r < h) ? A[row0 + r + (i64)c * lda] : 0.0;
         }
-        __syncthreads();
+    __syncwarp();
+
+    for (int j = 0; j < nc; ++j) {
+        double v[RPL];
+        double p = 0.0;
+#pragma unroll
+        for (int i = 0; i < RPL; ++i) {
+            const int r = lane + 32 * i;
+            v[i] = a[j * TR + r];
+            if (r > j) p = fma(v[i], v[i], p);
+        }
+        warp_sum<1>(&p);
+        const double alpha = a[j * TR + j];
+        double t = 0.0, beta = alpha, scal = 0.0;
+        if (p > 0.0) {
+            beta = -copysign(sqrt(alpha * alpha + p), alpha);
+            t = (beta - alpha) / beta;
+            scal = 1.0 / (alpha - beta);
+        }
+#pragma unroll
+        for (int i = 0; i < RPL; ++i) {
+            const int r = lane + 32 * i;
+            v[i] = (r > j) ? v[i] * scal : (r == j ? 1.0 : 0.0);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < RPL; ++i) {
+            const int r = lane + 32 * i;
+            if (r > j) a[j * TR + r] = v[i];
+            else if (r == j) a[j * TR + r] = beta;
+        }
+        if (lane == 0) tau[j] = t;
+        __syncwarp();
+        if (t != 0.0) {
+            int c = j + 1;
+            for (; c + 4 <= nc; c += 4) apply_reflector<RPL, 4>(a, TR, c, v, t, lane);
+            for (; c < nc; ++c) apply_reflector<RPL, 1>(a, TR, c, v, t, lane);
+        }
+        __syncwarp();
     }
     // R to the stack (upper, lower zero).
-    for (int e = r; e < nc * nc; e += TR) {
-        int i = e % nc, c = e / nc;
-        Rst[tile * nc + i + (i64)c * ldr] = (i <= c) ? a[i + c * TRP] : 0.0;
+    for (int e = lane; e < nc * nc; e += 32) {
+        const int i = e % nc, c = e / nc;
+        Rst[tile * nc + i + (i64)c * ldr] = (i <= c) ? a[c * TR + i] : 0.0;
     }
-    // Explicit Q = H_0 ... H_{nc-1} [I; 0] (dorg2r), backward accumulation.
-    for (int c = 0; c < NC; ++c) q[r + c * TRP] = (c < nc && r == c) ? 1.0 : 0.0;
-    __syncthreads();
+    __syncwarp();
+    // Explicit Q in place (dorg2r): for j = nc-1 .. 0, apply H_j to columns j+1..
+    // and set column j to (I - tau v v^T) e_j.
     for (int j = nc - 1; j >= 0; --j) {
-        const double tj = tau[j];
-        const double v = (r == j) ? 1.0 : ((r > j) ? a[r + j * TRP] : 0.0);
-        if (tj != 0.0) {
+        const double t = tau[j];
+        double v[RPL];
 #pragma unroll
-            for (int c = 0; c < NC; ++c)
-                if (c < nc) part[c] = v * q[r + c * TRP];
-            block_sum_vec<NC>(part, nc, red, wv);
-            if (r >= j)
-                for (int c = 0; c < nc; ++c) q[r + c * TRP] -= tj * wv[c] * v;
+        for (int i = 0; i < RPL; ++i) {
+            const int r = lane + 32 * i;
+            v[i] = (r > j) ? a[j * TR + r] : (r == j ? 1.0 : 0.0);
         }
-        __syncthreads();
+        if (t != 0.0) {
+            int c = j + 1;
+            for (; c + 4 <= nc; c += 4) apply_reflector<RPL, 4>(a, TR, c, v, t, lane);
+            for (; c < nc; ++c) apply_reflector<RPL, 1>(a, TR, c, v, t, lane);
+        }
+#pragma unroll
+        for (int i = 0; i < RPL; ++i) {
+            const int r = lane + 32 * i;
+            a[j * TR + r] = (r > j) ? -t * v[i] : (r == j ? 1.0 - t : 0.0);
+        }
+        __syncwarp();
     }
-    if (r < h)
-        for (int c = 0; c < nc; ++c) Q[row0 + r + (i64)c * ldq] = q[r + c * TRP];
-    __syncthreads();
+    for (int c = 0; c < nc; ++c)
+#pragma unroll
+        for (int i = 0; i < RPL; ++i) {
+            const int r = lane + 32 * i;
+            if (r < h) Q[row0 + r + (i64)c * ldq] = a[c * TR + r];
+        }
+    __syncwarp();
 }
 
 template <int NC>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32)
 tsqr_tile_kernel(const double* A, i64 lda, i64 rows, int nc, double* Q, i64 ldq,
                  double* __restrict__ Rst, i64 ldr) {
     extern __shared__ double smem[];
@@ -224,7 +250,7 @@ template <int NC>
 static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR, double* ws,
                     cudaStream_t st) {
     const int TR = tsqr_tile_rows(nc);
-    const size_t smem = (size_t)(2 * (TR + 1) * NC + TQ_MAXW * NC + 2 * NC) * sizeof(double);
+    const size_t smem = tsqr_tile_smem_bytes(TR, NC);
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(tsqr_tile_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -245,7 +271,7 @@ static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR
         const i64 tiles = ceil_div(lvl_rows[L], TR);
         double* next = cursor;
         cursor += tiles * nc * nc;
-        tsqr_tile_kernel<NC><<<(unsigned)tiles, TR, smem, st>>>(
+        tsqr_tile_kernel<NC><<<(unsigned)tiles, 32, smem, st>>>(
             lvl_ptr[L], lvl_ld[L], lvl_rows[L], nc, lvl_ptr[L], lvl_ld[L], next, tiles * nc);
         g_launch_count += 1;
         ++L;
@@ -255,7 +281,7 @@ static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR
     }
     // Root: one tile; its R goes to a small slot after the stacks.
     double* rroot = cursor;
-    tsqr_tile_kernel<NC><<<1, TR, smem, st>>>(lvl_ptr[L], lvl_ld[L], lvl_rows[L], nc, lvl_ptr[L],
+    tsqr_tile_kernel<NC><<<1, 32, smem, st>>>(lvl_ptr[L], lvl_ld[L], lvl_rows[L], nc, lvl_ptr[L],
                                               lvl_ld[L], rroot, nc);
     tsqr_root_fix<<<1, 256, 0, st>>>(lvl_ptr[L], lvl_ld[L], (int)lvl_rows[L], nc, rroot, nc, R, ldR);
     g_launch_count += 2;
@@ -284,11 +310,7 @@ int launch_tsqr(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR, do
 // down-sweep level over many panels (nc <= 16, TR = 256), with the single-panel
 // bodies.
 // ---------------------------------------------------------------------------
-static size_t tsqr_tile_smem_bytes(int TR, int NC) {
-    return (size_t)(2 * (TR + 1) * NC + TQ_MAXW * NC + 2 * NC) * sizeof(double);
-}
-
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32)
 tsqr_tile_batched(const TsqrTileJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
     extern __shared__ double smem[];
     const int j = batched_job_of(prefix, njobs, blockIdx.x);
@@ -327,7 +349,7 @@ int launch_tsqr_tile_batched(const TsqrTileJob* jobs, const int* prefix, int njo
     if (items <= 0) return 0;
     if (ncmax > 16) return (int)cudaErrorInvalidValue;
     const size_t smem = tsqr_tile_smem_bytes(256, 16);
-    tsqr_tile_batched<<<(unsigned)items, 256, smem, st>>>(jobs, prefix, njobs);
+    tsqr_tile_batched<<<(unsigned)items, 32, smem, st>>>(jobs, prefix, njobs);
     g_launch_count += 1;
     return (int)cudaGetLastError();
 }
