@@ -80,7 +80,7 @@ int orth_gb300_set_host_precision(int precision);
  */
 int orth_gb300_last_split_error(void);
 
-/* 1 if the split-precision mode handles (m, n, s) (s <= 32), else 0. */
+/* 1 if the split-precision mode handles (m, n, s) (s <= 64), else 0. */
 int orth_gb300_split_supported(int m, int n, int s);
 
 /*

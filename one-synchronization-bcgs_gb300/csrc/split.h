@@ -30,7 +30,7 @@ int split_error_word(int* out, cudaStream_t st);
 // A-ring waits, code + 100 * ring slot).
 int split_last_error();
 // Same contracts as launch_gram_fp64 / launch_update_fp64 (the update requires
-// c0 == K and nc <= 32).
+// c0 == K and nc <= 64; output columns are written in groups of 32).
 int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, double* out, int ldo,
                       char* ws, size_t ws_bytes, int num_sms, cudaStream_t st);
 int launch_update_split(double* X, i64 ld, i64 m, int K, int c0, int nc, const double* S, int lds,

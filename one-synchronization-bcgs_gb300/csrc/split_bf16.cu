@@ -216,9 +216,9 @@ __global__ void __launch_bounds__(256)
 bbuild_kernel(const double* __restrict__ S, int lds, const double* __restrict__ T, int ldt, int K, int nc,
               const int* __restrict__ cexp, double* __restrict__ Bp, int ldb,
               unsigned long long* __restrict__ bmax) {
-    __shared__ double ti[32][33];
+    __shared__ double ti[64][65];
     const int tid = threadIdx.x;
-    // T^{-1} (upper, nc x nc): column j solves T y = e_j by back substitution.
+    // T^{-1} (upper, nc x nc, nc <= 64): column j solves T y = e_j by back substitution.
     if (T != nullptr) {
         if (tid < nc) {
             const int j = tid;
@@ -229,7 +229,7 @@ bbuild_kernel(const double* __restrict__ S, int lds, const double* __restrict__ 
             }
         }
     } else {
-        for (int e = tid; e < 32 * 32; e += blockDim.x) ti[e / 32][e % 32] = (e / 32 == e % 32) ? 1.0 : 0.0;
+        for (int e = tid; e < 64 * 64; e += blockDim.x) ti[e / 64][e % 64] = (e / 64 == e % 64) ? 1.0 : 0.0;
     }
     __syncthreads();
     const int c = blockIdx.x * 64 + (tid & 63);
@@ -845,7 +845,7 @@ size_t layout_bytes(i64 m, int n, int s, int num_sms, Plan* out, char* base) {
     int* err = cv.take<int>(16);
     unsigned long long* cmax = cv.take<unsigned long long>(n + 64);
     unsigned long long* bmax = cv.take<unsigned long long>(64);
-    double* bfull = cv.take<double>(kpad * 32);
+    double* bfull = cv.take<double>(kpad * 64);
     const i64 pd = gram_part_doubles(m, n, s, num_sms);
     double* part = cv.take<double>(pd);
     if (out) {
@@ -894,7 +894,7 @@ int set_smem(K kernel, int bytes) {
 
 }  // namespace
 
-bool split_supported(i64 m, int n, int s) { return s >= 1 && s <= 32 && n >= 2 * s && m >= TILE_M; }
+bool split_supported(i64 m, int n, int s) { return s >= 1 && s <= 64 && n >= 2 * s && m >= TILE_M; }
 
 i64 split_workspace_bytes(i64 m, int n, int s, int num_sms) {
     return (i64)layout_bytes(m, n, s, num_sms, nullptr, nullptr);
@@ -1004,32 +1004,41 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
 
 // bdigit + the tensor-core product X[:, c0:c0+nc] = rowstore[:, 0:kin] * Bp, after the
 // caller has filled Bp/bmax.
+// Output columns go in groups of at most 32 (one tensor-core pass each). Every
+// group reads the same digit planes of X[:, 0:kin], which were sliced before the
+// first group wrote anything, and its own 32 columns of the factor in Bp.
 static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int num_sms, cudaStream_t st) {
     Plan& P = g_plan;
-    const int NB = nc <= 16 ? 16 : 32;
-    if (P.kd == 6)
-        bdigit_kernel<6><<<(unsigned)ceil_div(P.kpad, 256), 256, 0, st>>>(P.bfull, (int)P.kpad, kin - nc, nc, NB,
-                                                                           (int)P.kpad, P.bmax, P.fexp, P.bdig);
-    else
-        bdigit_kernel<7><<<(unsigned)ceil_div(P.kpad, 256), 256, 0, st>>>(P.bfull, (int)P.kpad, kin - nc, nc, NB,
-                                                                           (int)P.kpad, P.bmax, P.fexp, P.bdig);
-    cudaError_t ce = cudaMemsetAsync(P.cmax + c0, 0, (size_t)nc * sizeof(unsigned long long), st);
-    if (ce != cudaSuccess) return (int)ce;
-    UpdateParams up;
-    up.ncc = (int)P.ncc;
-    up.m = m; up.kin = kin; up.nc = nc; up.c0 = c0; up.ld = ld; up.X = X; up.fexp = P.fexp;
-    up.cmax = P.cmax; up.err = P.err;
-    const int ntiles = (int)ceil_div(m, TILE_M);
-    const int grid = ntiles < num_sms ? ntiles : num_sms;
+    for (int j0 = 0; j0 < nc; j0 += 32) {
+        const int ng = nc - j0 < 32 ? nc - j0 : 32;
+        const int NB = ng <= 16 ? 16 : 32;
+        const double* Bg = P.bfull + (i64)j0 * P.kpad;
+        if (P.kd == 6)
+            bdigit_kernel<6><<<(unsigned)ceil_div(P.kpad, 256), 256, 0, st>>>(Bg, (int)P.kpad, kin - ng, ng, NB,
+                                                                               (int)P.kpad, P.bmax + j0, P.fexp,
+                                                                               P.bdig);
+        else
+            bdigit_kernel<7><<<(unsigned)ceil_div(P.kpad, 256), 256, 0, st>>>(Bg, (int)P.kpad, kin - ng, ng, NB,
+                                                                               (int)P.kpad, P.bmax + j0, P.fexp,
+                                                                               P.bdig);
+        cudaError_t ce = cudaMemsetAsync(P.cmax + c0 + j0, 0, (size_t)ng * sizeof(unsigned long long), st);
+        if (ce != cudaSuccess) return (int)ce;
+        UpdateParams up;
+        up.ncc = (int)P.ncc;
+        up.m = m; up.kin = kin; up.nc = ng; up.c0 = c0 + j0; up.ld = ld; up.X = X; up.fexp = P.fexp;
+        up.cmax = P.cmax; up.err = P.err;
+        const int ntiles = (int)ceil_div(m, TILE_M);
+        const int grid = ntiles < num_sms ? ntiles : num_sms;
 #define BCGS_UPD(NBT, KDT) \
-    update_tc_kernel<NBT, KDT><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(P.map_row_a, P.map_bdig##NBT, up)
-    if (NB == 16) {
-        if (P.kd == 6) BCGS_UPD(16, 6); else BCGS_UPD(16, 7);
-    } else {
-        if (P.kd == 6) BCGS_UPD(32, 6); else BCGS_UPD(32, 7);
-    }
+        update_tc_kernel<NBT, KDT><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(P.map_row_a, P.map_bdig##NBT, up)
+        if (NB == 16) {
+            if (P.kd == 6) BCGS_UPD(16, 6); else BCGS_UPD(16, 7);
+        } else {
+            if (P.kd == 6) BCGS_UPD(32, 6); else BCGS_UPD(32, 7);
+        }
 #undef BCGS_UPD
-    g_launch_count += 2;
+        g_launch_count += 2;
+    }
     for (int c = c0; c < c0 + nc; ++c) { P.fresh[c] = 0; P.cmax_valid[c] = 1; }
     return (int)cudaGetLastError();
 }
@@ -1039,7 +1048,7 @@ int launch_update_split(double* X, i64 ld, i64 m, int K, int c0, int nc, const d
     (void)ws; (void)ws_bytes;
     Plan& P = g_plan;
     if (nc <= 0) return 0;
-    if (c0 != K || nc > 32 || X != P.X) return (int)cudaErrorInvalidValue;
+    if (c0 != K || nc > 64 || X != P.X) return (int)cudaErrorInvalidValue;
     int rc = ensure_fresh(0, K + nc, st);
     if (rc) return rc;
     cudaError_t ce = cudaMemsetAsync(P.bmax, 0, 64 * sizeof(unsigned long long), st);

@@ -258,7 +258,7 @@ static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR
         attr_set = true;
     }
     // Level matrices: level 0 is the panel itself; level l >= 1 lives in ws.
-    constexpr int kMaxLevels = 16;
+    constexpr int kMaxLevels = 48;   // nc > 32 reduces 128 rows to 64 per level: 2^k rows need about k levels
     double* lvl_ptr[kMaxLevels];
     i64 lvl_rows[kMaxLevels], lvl_ld[kMaxLevels];
     lvl_ptr[0] = X + (i64)c0 * ld;

@@ -94,3 +94,25 @@ def test_split_bit_exact_run_to_run(lib):
         assert rc == 0
         res.append((dX.cpu().numpy(), dR.cpu().numpy()))
     assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("s", [32, 64])
+def test_split_wide_blocks(lib, variant, s):
+    """s = 32 and 64 (config-3 block sizes): the update writes its output columns in
+    groups of 32 over one digit store; the 56-bit form stays within 10x of FP64."""
+    torch = pytest.importorskip("torch")
+    m, n = 60000, 4 * s
+    X = inputs.graded_host(m, n, 1e6, seed=s + 1)
+    st = torch.cuda.current_stream().cuda_stream
+    assert orth.split_supported(m, n, s)
+    out = {}
+    for prec in (orth.FP64, orth.SPLIT_BF16):
+        dX = _dev(torch, X)
+        dR = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        rc, status = orth.run_dev(variant, m, n, s, dX.data_ptr(), m, dR.data_ptr(), n, prec, st)
+        assert rc == 0 and status["breakdown_step"] == 0 and status["timeout"] == 0, (rc, status)
+        out[prec] = (dX.cpu().numpy().T.copy(), dR.cpu().numpy().T.copy())
+    (Q, R), (Qf, Rf) = out[orth.SPLIT_BF16], out[orth.FP64]
+    assert port.loo_2(Q) <= 10 * max(port.loo_2(Qf), 1e-15)
+    assert port.rel_residual(X, Q, np.triu(R)) <= 10 * max(port.rel_residual(X, Qf, np.triu(Rf)), 1e-15)
