@@ -58,6 +58,7 @@ struct Context {
     double* hostR_stage = nullptr;
     size_t hostR_stage_bytes = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;   // host-path column transfers
     int num_sms = kNumSMsDefault;
     bool init = false;
 };
@@ -133,6 +134,8 @@ int init_ctx() {
     BCGS_CUDA_TRY(cudaGetDevice(&dev));
     BCGS_CUDA_TRY(cudaDeviceGetAttribute(&g_ctx.num_sms, cudaDevAttrMultiProcessorCount, dev));
     BCGS_CUDA_TRY(cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking));
+    BCGS_CUDA_TRY(cudaStreamCreateWithFlags(&g_ctx.copy_in, cudaStreamNonBlocking));
+    BCGS_CUDA_TRY(cudaStreamCreateWithFlags(&g_ctx.copy_out, cudaStreamNonBlocking));
     g_ctx.init = true;
     return 0;
 }
@@ -194,6 +197,71 @@ int reserve(i64 m, int n, int s, int precision) {
 }
 
 // ---------------------------------------------------------------------------
+// Host-buffer runs (the orth.h entry points): X arrives in column chunks on one
+// copy stream and Q leaves on another while the QR runs. The compute stream waits
+// only for the chunks a primitive reads (need). Every update or TSQR that writes
+// from column c0 marks columns [0, c0) final (final). No variant writes a column
+// left of the block it is working on, so those columns can be copied back at once.
+// ---------------------------------------------------------------------------
+struct HostLink {
+    double* hX = nullptr;   // caller's X (host), ld ldh
+    i64 ldh = 0, m = 0;
+    int n = 0, chunk = 1;
+    double* dX = nullptr;   // device copy, ld m
+    cudaStream_t cin = nullptr, cout = nullptr;
+    std::vector<cudaEvent_t> ev_in;
+    cudaEvent_t ev_fin = nullptr;
+    int waited = 0, out_done = 0, err = 0;
+
+    cudaError_t copy(double* dst, i64 ldd, const double* src, i64 lds, int c0, int nc, cudaMemcpyKind kind,
+                     cudaStream_t s) {
+        const size_t w = (size_t)m * sizeof(double);
+        if (ldd == m && lds == m)
+            return cudaMemcpyAsync(dst + (i64)c0 * ldd, src + (i64)c0 * lds, w * nc, kind, s);
+        return cudaMemcpy2DAsync(dst + (i64)c0 * ldd, (size_t)ldd * sizeof(double), src + (i64)c0 * lds,
+                                 (size_t)lds * sizeof(double), w, (size_t)nc, kind, s);
+    }
+    // Enqueue every H2D chunk on cin (after `st` reaches this point).
+    void start(cudaStream_t st) {
+        cudaEvent_t e0 = nullptr;
+        if ((err = (int)cudaEventCreateWithFlags(&e0, cudaEventDisableTiming))) return;
+        cudaEventRecord(e0, st);
+        cudaStreamWaitEvent(cin, e0, 0);
+        cudaStreamWaitEvent(cout, e0, 0);
+        cudaEventDestroy(e0);
+        if ((err = (int)cudaEventCreateWithFlags(&ev_fin, cudaEventDisableTiming))) return;
+        for (int c0 = 0; c0 < n && !err; c0 += chunk) {
+            const int nc = n - c0 < chunk ? n - c0 : chunk;
+            cudaEvent_t e = nullptr;
+            if ((err = (int)cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) break;
+            ev_in.push_back(e);
+            if ((err = (int)copy(dX, m, hX, ldh, c0, nc, cudaMemcpyHostToDevice, cin))) break;
+            err = (int)cudaEventRecord(e, cin);
+        }
+    }
+    void need(cudaStream_t st, int c_end) {
+        while (!err && waited < c_end && waited < n) {
+            err = (int)cudaStreamWaitEvent(st, ev_in[waited / chunk], 0);
+            waited = (waited / chunk + 1) * chunk;
+        }
+    }
+    void final(cudaStream_t st, int c_end) {
+        if (err || c_end <= out_done) return;
+        if (c_end > n) c_end = n;
+        err = (int)cudaEventRecord(ev_fin, st);
+        if (!err) err = (int)cudaStreamWaitEvent(cout, ev_fin, 0);
+        if (!err) err = (int)copy(hX, ldh, dX, m, out_done, c_end - out_done, cudaMemcpyDeviceToHost, cout);
+        out_done = c_end;
+    }
+    void release() {
+        for (cudaEvent_t e : ev_in) cudaEventDestroy(e);
+        ev_in.clear();
+        if (ev_fin) cudaEventDestroy(ev_fin);
+        ev_fin = nullptr;
+    }
+};
+
+// ---------------------------------------------------------------------------
 // Per-call engine: the primitives every variant is written in.
 // ---------------------------------------------------------------------------
 struct Engine {
@@ -208,10 +276,20 @@ struct Engine {
     Small w;
     int* status;
     int err = 0;
+    HostLink* link = nullptr;   // host-buffer runs only
+
+    // X columns [0, c_end) must be on the device; columns [0, c_fin) are final.
+    void host_sync(int c_end, int c_fin) {
+        if (!link || err) return;
+        link->need(st, c_end);
+        if (c_fin >= 0) link->final(st, c_fin);
+        if (link->err) err = link->err;
+    }
 
     // C (na x nb, ld na) = X[:, 0:na]^T X[:, b0:b0+nb]: one synchronization.
     void gram(int na, int b0, int nb, double* C) {
         if (err || na <= 0 || nb <= 0) return;
+        host_sync(na > b0 + nb ? na : b0 + nb, -1);
         if (is_split(precision)) {
             ProfScope pslice(4, st, 0.0, 0.0);
             err = split_prepare(na > b0 + nb ? na : b0 + nb, st);
@@ -230,6 +308,7 @@ struct Engine {
     // X[:, c0:c0+nc] = (X[:, c0:c0+nc] - X[:, 0:K] S) T^{-1}
     void update(int K, int c0, int nc, const double* S, int lds, const double* T, int ldt) {
         if (err || nc <= 0) return;
+        host_sync(K > c0 + nc ? K : c0 + nc, c0);
         if (is_split(precision)) {
             ProfScope pslice(4, st, 0.0, 0.0);
             err = split_prepare(K + nc, st);
@@ -249,6 +328,7 @@ struct Engine {
     void fused_update(int K, int nz, const double* G, int ldg, const double* Ty, const double* Sp,
                       const double* Ts) {
         if (err) return;
+        host_sync(K + s + nz, K);
         {
             ProfScope pslice(4, st, 0.0, 0.0);
             err = split_prepare(K + s + nz, st);
@@ -278,6 +358,7 @@ struct Engine {
     // Explicit TSQR of X[:, c0:c0+nc]; R into (Rout, ldr).
     void tsqr(int c0, int nc, double* Rout, int ldr) {
         if (err) return;
+        host_sync(c0 + nc, c0);
         ProfScope ps(3, st, 6.0 * m * nc * nc, 8.0 * m * nc * 3.0);
         err = launch_tsqr(X, ld, m, c0, nc, Rout, ldr, g_ctx.tsqr.as<double>(), st);
         if (is_split(precision)) split_mark_stale(c0, nc);
@@ -544,7 +625,7 @@ bool valid_args(int m, int n, int s, long long ldX, int ldR) {
 }
 
 int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR, int ldR,
-               int precision, cudaStream_t st, orth_gb300_status* out) {
+               int precision, cudaStream_t st, orth_gb300_status* out, HostLink* link = nullptr) {
     if (!valid_args(m, n, s, ldX, ldR)) return 2;
     if (variant < 0 || variant > 4) return 2;
     if (precision != ORTH_GB300_FP64 && !is_split(precision)) return 4;
@@ -557,6 +638,7 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
     const long long launches0 = g_launch_count;
     Engine e{dX, (i64)ldX, (i64)m, n, s, dR, ldR, precision, st,
              carve_small(g_ctx.small.as<double>(), n, s), g_ctx.status.as<int>()};
+    e.link = link;
     cudaError_t ce = cudaMemsetAsync(e.status, 0, kStatusWords * sizeof(int), st);
     if (ce != cudaSuccess) e.err = (int)ce;
     if (!e.err && is_split(precision))
@@ -628,25 +710,38 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
     double* dR = g_ctx.hostR.as<double>();
     orth_gb300_status stt;
     std::memset(&stt, 0, sizeof(stt));
-    cudaError_t ce = cudaMemcpy2DAsync(dX, (size_t)m * sizeof(double), Xsub,
-                                       (size_t)ldXsub * sizeof(double), (size_t)m * sizeof(double),
-                                       (size_t)n, cudaMemcpyHostToDevice, st);
-    if (ce == cudaSuccess) ce = cudaMemsetAsync(dR, 0, rbytes, st);
-    if (ce != cudaSuccess) {
-        stt.cuda_error = (int)ce;
-        g_last_status = stt;
-        return 3;
+    // X goes up in column chunks of at least one block and about 64 MB on a copy
+    // stream; Q comes back on another as its columns become final (HostLink).
+    HostLink link;
+    link.hX = Xsub; link.ldh = ldXsub; link.m = m; link.n = n; link.dX = dX;
+    link.cin = g_ctx.copy_in; link.cout = g_ctx.copy_out;
+    {
+        const i64 per64mb = ((i64)64 << 20) / ((i64)m * (i64)sizeof(double));
+        link.chunk = (int)(per64mb > s ? (per64mb < n ? per64mb : n) : s);
     }
-    rc = run_device(variant, m, n, s, dX, m, dR, n, precision, st, &stt);
+    cudaError_t ce = cudaMemsetAsync(dR, 0, rbytes, st);
+    if (ce == cudaSuccess) {
+        link.start(st);
+        ce = (cudaError_t)link.err;
+    }
+    if (ce == cudaSuccess) {
+        rc = run_device(variant, m, n, s, dX, m, dR, n, precision, st, &stt, &link);
+        if (!rc) {
+            link.final(st, n);
+            ce = (cudaError_t)link.err;
+            if (ce == cudaSuccess) ce = cudaMemcpyAsync(g_ctx.hostR_stage, dR, rbytes, cudaMemcpyDeviceToHost, st);
+        }
+    }
+    // The caller's buffer is in use until both copy streams are done, on every path.
+    cudaError_t c1 = cudaStreamSynchronize(g_ctx.copy_in);
+    cudaError_t c2 = cudaStreamSynchronize(g_ctx.copy_out);
+    cudaError_t c3 = cudaStreamSynchronize(st);
+    link.release();
+    if (ce == cudaSuccess) ce = c1 != cudaSuccess ? c1 : (c2 != cudaSuccess ? c2 : c3);
     if (rc) {
         g_last_status = stt;
         return rc;
     }
-    ce = cudaMemcpy2DAsync(Xsub, (size_t)ldXsub * sizeof(double), dX, (size_t)m * sizeof(double),
-                           (size_t)m * sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, st);
-    if (ce == cudaSuccess)
-        ce = cudaMemcpyAsync(g_ctx.hostR_stage, dR, rbytes, cudaMemcpyDeviceToHost, st);
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) {
         stt.cuda_error = (int)ce;
         g_last_status = stt;
