@@ -133,12 +133,14 @@ __global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c
 }
 
 // Slice columns [c0, c0+nc) of X into both digit stores. A CTA handles 128 rows x
-// 8 columns (grid: row tiles x column groups), one row per thread: 8 coalesced
-// column loads, the digits, one 16-byte row-store piece per plane, and the
-// column-store planes staged in shared memory so they leave as 16-byte stores
-// along the rows. Small CTAs keep many loads in flight per SM.
+// 16 columns (grid: row tiles x column groups), one row per thread: 16 coalesced
+// column loads and the digits, staged in shared memory as [plane][column][row].
+// Both stores are then written from the staging in whole 32-byte sectors:
+//   * column store: per (plane, column) two 128-byte runs (64 rows each);
+//   * row store: per (plane, row) one 32-byte sector (16 columns), written by a
+//     pair of lanes, so one warp store covers 16 complete sectors.
 template <int KD>
-__global__ void __launch_bounds__(128, 4)
+__global__ void __launch_bounds__(128, 6)
 slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
              const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
              unsigned short* __restrict__ colstore, i64 nrc, unsigned short* __restrict__ rowstore, i64 ncc) {
@@ -152,46 +154,39 @@ slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
     double x[CG];
 #pragma unroll
     for (int j = 0; j < CG; ++j) x[j] = (g + j < nc && r < m) ? X[r + (i64)(c0 + g + j) * ld] : 0.0;
-    uint32_t packed[KD][CG / 2];
 #pragma unroll
-    for (int j = 0; j < CG; j += 2) {
-        int d0[KD], d1[KD];
-        split_digits<KD>(x[j], g + j < nc ? scale_exp(cmax[c0 + g + j]) : 0, d0);
-        split_digits<KD>(x[j + 1], g + j + 1 < nc ? scale_exp(cmax[c0 + g + j + 1]) : 0, d1);
+    for (int j = 0; j < CG; ++j) {
+        int d[KD];
+        split_digits<KD>(x[j], g + j < nc ? scale_exp(cmax[c0 + g + j]) : 0, d);
 #pragma unroll
-        for (int i = 0; i < KD; ++i) {
-            const unsigned short b0 = bf16_bits_of_int(d0[i]), b1 = bf16_bits_of_int(d1[i]);
-            packed[i][j / 2] = (uint32_t)b0 | ((uint32_t)b1 << 16);
-            sdig[i][j][t] = b0;
-            sdig[i][j + 1][t] = b1;
-        }
-    }
-    // Row store: element (r, c) of plane i at ((i*ncc + c/64)*m + r)*64 + c%64.
-    if (r < m) {
-        const int cb = c0 + g;
-        const bool vec = (g + CG <= nc) && ((cb & 15) == 0);   // 16 columns in one 64-column chunk
-#pragma unroll
-        for (int i = 0; i < KD; ++i) {
-            if (vec) {
-                unsigned short* dst = rowstore + (((i64)i * ncc + cb / 64) * m + r) * 64 + (cb & 63);
-                uint4* d4 = reinterpret_cast<uint4*>(dst);
-                d4[0] = make_uint4(packed[i][0], packed[i][1], packed[i][2], packed[i][3]);
-                d4[1] = make_uint4(packed[i][4], packed[i][5], packed[i][6], packed[i][7]);
-            } else {
-#pragma unroll
-                for (int j = 0; j < CG; ++j) {
-                    const int c = cb + j;
-                    if (g + j < nc)
-                        rowstore[(((i64)i * ncc + c / 64) * m + r) * 64 + (c & 63)] =
-                            (unsigned short)((packed[i][j / 2] >> (16 * (j & 1))) & 0xFFFFu);
-                }
-            }
-        }
+        for (int i = 0; i < KD; ++i) sdig[i][j][t] = bf16_bits_of_int(d[i]);
     }
     __syncthreads();
+    const bool full = (r0 + 128 <= m);
+    // Row store: element (r, c) of plane i at ((i*ncc + c/64)*m + r)*64 + c%64.
+    const int cb = c0 + g;
+    const bool vec = (g + CG <= nc) && ((cb & 15) == 0);   // 16 columns in one 64-column chunk
+    if (vec && full) {
+        for (int e = t; e < KD * 128 * 2; e += 128) {
+            const int i = e >> 8, rr = (e & 255) >> 1, h = e & 1;
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                w[q] = (uint32_t)sdig[i][8 * h + 2 * q][rr] | ((uint32_t)sdig[i][8 * h + 2 * q + 1][rr] << 16);
+            unsigned short* dst = rowstore + (((i64)i * ncc + cb / 64) * m + r0 + rr) * 64 + (cb & 63) + 8 * h;
+            *reinterpret_cast<uint4*>(dst) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    } else if (r < m) {
+#pragma unroll
+        for (int i = 0; i < KD; ++i)
+#pragma unroll
+            for (int j = 0; j < CG; ++j) {
+                const int c = cb + j;
+                if (g + j < nc) rowstore[(((i64)i * ncc + c / 64) * m + r) * 64 + (c & 63)] = sdig[i][j][t];
+            }
+    }
     // Column store: element (r, c) of plane i at ((i*nrc + r/64)*n + c)*64 + r%64; per
     // (plane, column) the CTA's 128 rows are two 128-byte runs = 16 pieces of 16 bytes.
-    const bool full = (r0 + 128 <= m);
     for (int e = t; e < KD * CG * 16; e += 128) {
         const int piece = e & 15, ij = e >> 4;
         const int i = ij / CG, j = ij % CG;
