@@ -124,15 +124,26 @@ void orth_gb300_set_gram_chunk_rows(long long rows);
  * Matrix b: dX[b] (m[b] x n[b], ldX[b] >= m[b], overwritten with Q), dR[b]
  * (n[b] x n[b], ldR[b]; upper block triangle written), block size s[b] <= 16,
  * n[b] >= 2 s[b], m[b] >= n[b]. Arrays are host arrays of count entries (ldX/ldR
- * may be NULL: tight). precision: ORTH_GB300_FP64. variant: ORTH_GB300_BCGSI2P1S.
- * flags: ORTH_GB300_BATCH_TUNE times the Gram's panel width and chunk rows per
- * block size on the batch itself (reads X, writes only the plan's scratch).
+ * may be NULL: tight). precision ORTH_GB300_FP64: variant ORTH_GB300_BCGSI2P1S,
+ * s[b] <= 16. flags: ORTH_GB300_BATCH_TUNE times the Gram's panel width and chunk
+ * rows per block size on the batch itself (reads X, writes only the plan's
+ * scratch).
+ * precision ORTH_GB300_SPLIT_BF16 / _FAST: any variant, s[b] <= 64. Each run
+ * spreads the matrices over up to 8 scratch slots (longest first to the least
+ * loaded slot), each on its own stream forked from and joined back into `stream`,
+ * and runs them through the single-matrix tensor-core driver (no graph; a slot's
+ * digit stores, 28 bytes per element, are sized for its largest matrix and
+ * reused). Breakdowns and split-kernel timeouts are collected per matrix on the
+ * device. The slots are the library's own scratch: order any later library call
+ * after the run (same stream, or a synchronize).
  * The plan owns its device workspace; runs must not overlap.
  * Returns 0, 2 (invalid arguments), 3 (CUDA failure), 4 (variant/precision not
  * available in batched form).
  */
 typedef struct orth_gb300_batch orth_gb300_batch;
 #define ORTH_GB300_BATCH_TUNE 1
+/* Split-precision batches: use one stream and one scratch slot (less device memory). */
+#define ORTH_GB300_BATCH_ONE_STREAM 2
 int orth_gb300_batch_create(orth_gb300_batch **plan, int variant, int count, const int *m, const int *n,
                             const int *s, double *const *dX, const long long *ldX, double *const *dR,
                             const int *ldR, int precision, int flags, void *stream);
@@ -149,6 +160,13 @@ void orth_gb300_batch_destroy(orth_gb300_batch *plan);
  * for these shapes would hold. */
 int orth_gb300_batch_dry_run(int count, const int *m, const int *n, const int *s, long long *stages,
                              long long *launches_per_run, long long *workspace_bytes);
+
+/*
+ * Diagnostic: fill every SM's shared memory with the 64-bit pattern `bits` (e.g. a
+ * NaN), on `stream`. A later kernel that reads shared memory it did not write
+ * then reads that pattern, so such reads become visible in results. 0 or 3.
+ */
+int orth_gb300_poison_shared_memory(unsigned long long bits, void *stream);
 
 /* Status of the last run through the orth.h entry points on this thread. */
 void orth_gb300_last_status(orth_gb300_status *status);

@@ -91,6 +91,8 @@ def load(path: str | None = None):
                                             ctypes.POINTER(ctypes.c_double)]
     lib.orth_gb300_accuracy_dev.restype = ctypes.c_int
     lib.orth_gb300_set_gram_chunk_rows.argtypes = [ctypes.c_longlong]
+    lib.orth_gb300_poison_shared_memory.argtypes = [ctypes.c_ulonglong, ctypes.c_void_p]
+    lib.orth_gb300_poison_shared_memory.restype = ctypes.c_int
     lib.orth_gb300_set_gram_chunk_rows.restype = None
     P_int, P_ll, P_vp = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_void_p)
     lib.orth_gb300_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, P_int, P_int,
@@ -221,12 +223,18 @@ def accuracy_dev(m: int, n: int, x_ptr: int, ldx: int, q_ptr: int, ldq: int, r_p
     return rc, float(out[0]), float(out[1]), float(out[2])
 
 
+def poison_shared_memory(bits: int = 0x7FF8DEADBEEF0001, stream: int = 0) -> int:
+    """Fill every SM's shared memory with a 64-bit pattern (default: a quiet NaN)."""
+    return int(load().orth_gb300_poison_shared_memory(bits, ctypes.c_void_p(stream)))
+
+
 def set_gram_chunk_rows(rows: int) -> None:
     """Rows per FP64 Gram chunk (0 restores the default chunking policy)."""
     load().orth_gb300_set_gram_chunk_rows(int(rows))
 
 
 BATCH_TUNE = 1
+BATCH_ONE_STREAM = 2
 
 
 def _int_array(v):
@@ -250,7 +258,7 @@ class Batch:
     """
 
     def __init__(self, ms, ns, ss, x_ptrs, r_ptrs, ldx=None, ldr=None, precision=FP64, tune=True,
-                 stream: int = 0, variant: str = "bcgsi2P1s"):
+                 stream: int = 0, variant: str = "bcgsi2P1s", one_stream: bool = False):
         lib = load()
         self.count = len(ms)
         self._h = ctypes.c_void_p(0)
@@ -260,7 +268,8 @@ class Batch:
         lr = _int_array(ldr if ldr is not None else ns)
         self.rc = int(lib.orth_gb300_batch_create(ctypes.byref(self._h), VARIANT_ID[variant], self.count,
                                                   _int_array(ms), _int_array(ns), _int_array(ss), xs, lx, rs, lr,
-                                                  precision, BATCH_TUNE if tune else 0, ctypes.c_void_p(stream)))
+                                                  precision, (BATCH_TUNE if tune else 0) | (BATCH_ONE_STREAM if one_stream else 0),
+                                                  ctypes.c_void_p(stream)))
 
     def run(self, stream: int = 0) -> int:
         return int(load().orth_gb300_batch_run(self._h, ctypes.c_void_p(stream)))

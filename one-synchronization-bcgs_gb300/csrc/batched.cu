@@ -36,6 +36,10 @@
 namespace bcgs {
 
 int tsqr_tile_batched_prepare();
+int split_batch_enqueue(int variant, int count, const int* m, const int* n, const int* s, double* const* dX,
+                        const long long* ldX, double* const* dR, const int* ldR, int precision, cudaStream_t st,
+                        int* dstatus, int max_slots);
+bool split_supported(i64 m, int n, int s);
 
 namespace {
 
@@ -117,6 +121,13 @@ struct BatchPlan {
     cudaGraphExec_t exec = nullptr;
     long long launches = 0;
     int graph_nodes = 0;
+    // Split-precision batches run the single-matrix driver per matrix (no graph).
+    bool split = false;
+    int variant = 0, precision = 0, max_slots = 0;
+    std::vector<int> vm, vn, vs, vldR;
+    std::vector<double*> vX, vR;
+    std::vector<long long> vldX;
+    int* dstatus = nullptr;   // 8 ints per matrix: status words, split error word
 };
 
 namespace {
@@ -568,6 +579,7 @@ int autotune(BatchPlan& P, cudaStream_t st) {
 
 void free_plan(BatchPlan* P) {
     if (!P) return;
+    if (P->dstatus) cudaFree(P->dstatus);
     if (P->exec) cudaGraphExecDestroy(P->exec);
     if (P->graph) cudaGraphDestroy(P->graph);
     if (P->jobs_dev) cudaFree(P->jobs_dev);
@@ -610,9 +622,30 @@ int orth_gb300_batch_create(orth_gb300_batch** out, int variant, int count, cons
     if (!out) return 2;
     *out = nullptr;
     if (count < 1 || !m || !n || !s || !dX || !dR) return 2;
-    if (variant != ORTH_GB300_BCGSI2P1S || precision != ORTH_GB300_FP64) return 4;
     for (int b = 0; b < count; ++b)
         if (!dX[b] || !dR[b]) return 2;
+    if (precision == ORTH_GB300_SPLIT_BF16 || precision == ORTH_GB300_SPLIT_BF16_FAST) {
+        if (variant < ORTH_GB300_BCGSI2P1S || variant > ORTH_GB300_BCGSI2P2S) return 4;
+        BatchPlan* P = new BatchPlan();
+        P->split = true; P->variant = variant; P->precision = precision; P->count = count;
+        P->max_slots = (flags & ORTH_GB300_BATCH_ONE_STREAM) ? 1 : 0;
+        for (int b = 0; b < count; ++b) {
+            const long long lx = ldX ? ldX[b] : m[b];
+            const int lr = ldR ? ldR[b] : n[b];
+            if (s[b] < 1 || n[b] < 2 * s[b] || m[b] < n[b] || lx < m[b] || lr < n[b]) { free_plan(P); return 2; }
+            if (!split_supported(m[b], n[b], s[b])) { free_plan(P); return 4; }
+            P->vm.push_back(m[b]); P->vn.push_back(n[b]); P->vs.push_back(s[b]);
+            P->vX.push_back(dX[b]); P->vR.push_back(dR[b]); P->vldX.push_back(lx); P->vldR.push_back(lr);
+        }
+        if (cudaMalloc(&P->dstatus, (size_t)count * 8 * sizeof(int)) != cudaSuccess ||
+            cudaMemset(P->dstatus, 0, (size_t)count * 8 * sizeof(int)) != cudaSuccess) {
+            free_plan(P);
+            return 3;
+        }
+        *out = new orth_gb300_batch{P};
+        return 0;
+    }
+    if (variant != ORTH_GB300_BCGSI2P1S || precision != ORTH_GB300_FP64) return 4;
     BatchPlan* P = new BatchPlan();
     int rc = fill_mats(*P, count, m, n, s, dX, ldX, dR, ldR);
     if (rc) { free_plan(P); return rc; }
@@ -646,8 +679,18 @@ int orth_gb300_batch_create(orth_gb300_batch** out, int variant, int count, cons
 }
 
 int orth_gb300_batch_run(orth_gb300_batch* h, void* stream) {
-    if (!h || !h->plan || !h->plan->exec) return 2;
+    if (!h || !h->plan) return 2;
     cudaStream_t st = (cudaStream_t)stream;
+    if (h->plan->split) {
+        BatchPlan& P = *h->plan;
+        const long long l0 = bcgs::g_launch_count;
+        const int rc = bcgs::split_batch_enqueue(P.variant, P.count, P.vm.data(), P.vn.data(), P.vs.data(),
+                                                 P.vX.data(), P.vldX.data(), P.vR.data(), P.vldR.data(),
+                                                 P.precision, st, P.dstatus, P.max_slots);
+        P.launches = bcgs::g_launch_count - l0;
+        return rc;
+    }
+    if (!h->plan->exec) return 2;
     if (cudaGraphLaunch(h->plan->exec, st) != cudaSuccess) return 3;
     bcgs::g_launch_count += h->plan->launches;
     return 0;
@@ -657,16 +700,19 @@ int orth_gb300_batch_status(orth_gb300_batch* h, int* breakdown_step, int* break
     using namespace bcgs;
     if (!h || !h->plan) return 2;
     BatchPlan& P = *h->plan;
-    std::vector<int> st((size_t)P.count * kStatusWords);
     if (cudaDeviceSynchronize() != cudaSuccess) return 3;
-    if (cudaMemcpy(st.data(), P.mats[0].status, st.size() * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
-        return 3;
-    int broken = 0;
+    const int stride = P.split ? 8 : kStatusWords;
+    std::vector<int> st((size_t)P.count * stride);
+    const int* src = P.split ? P.dstatus : P.mats[0].status;
+    if (cudaMemcpy(st.data(), src, st.size() * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return 3;
+    int broken = 0, timeouts = 0;
     for (int b = 0; b < P.count; ++b) {
-        if (breakdown_step) breakdown_step[b] = st[(size_t)b * kStatusWords];
-        if (breakdown_info) breakdown_info[b] = st[(size_t)b * kStatusWords + 1];
-        if (st[(size_t)b * kStatusWords]) ++broken;
+        if (breakdown_step) breakdown_step[b] = st[(size_t)b * stride];
+        if (breakdown_info) breakdown_info[b] = st[(size_t)b * stride + 1];
+        if (st[(size_t)b * stride]) ++broken;
+        if (P.split && st[(size_t)b * stride + 4]) ++timeouts;
     }
+    if (timeouts) return 3;   // a bounded wait of the split kernels ran out
     if (nbroken) *nbroken = broken;
     return 0;
 }

@@ -5,6 +5,7 @@
 // sequence of operations (cited per line), with MPI_Allreduce replaced by one
 // deterministic device-wide reduction and every small s x s step kept on the
 // device, so a whole QR is enqueued on one stream with no host round trip.
+#include <algorithm>
 #include <climits>
 #include <cstdio>
 #include <cstdlib>
@@ -53,8 +54,19 @@ struct DevBuf {
 
 // Cached workspace (grow-only). The reference is not thread-safe either (it uses
 // MPI_COMM_WORLD collectives); calls are serialized by a mutex here.
+// Per-call scratch of the drivers. Slot 0 serves every entry point; split-precision
+// batches use up to kSlots slots, one per concurrent stream.
+constexpr int kSlots = 8;
+struct Scratch {
+    DevBuf part, small, status, tsqr, split;
+};
+Scratch g_scratch[kSlots];
+int g_slot = 0;
+inline Scratch& scr() { return g_scratch[g_slot]; }
+
 struct Context {
-    DevBuf part, gram, small, status, tsqr, hostX, hostR, split, metric;
+    DevBuf gram, hostX, hostR, metric;
+    cudaStream_t slot_stream[kSlots] = {};
     double* hostR_stage = nullptr;
     size_t hostR_stage_bytes = 0;
     cudaStream_t stream = nullptr;
@@ -181,16 +193,16 @@ Small carve_small(double* base, int n, int s) {
 int reserve(i64 m, int n, int s, int precision) {
     int rc = init_ctx();
     if (rc) return rc;
-    rc = g_ctx.part.ensure((size_t)part_doubles(m, n, s, g_ctx.num_sms) * sizeof(double));
+    rc = scr().part.ensure((size_t)part_doubles(m, n, s, g_ctx.num_sms) * sizeof(double));
     if (rc) return rc;
-    rc = g_ctx.small.ensure((size_t)small_doubles(n, s) * sizeof(double));
+    rc = scr().small.ensure((size_t)small_doubles(n, s) * sizeof(double));
     if (rc) return rc;
-    rc = g_ctx.status.ensure(kStatusWords * sizeof(int));
+    rc = scr().status.ensure(kStatusWords * sizeof(int));
     if (rc) return rc;
-    rc = g_ctx.tsqr.ensure((size_t)tsqr_workspace_doubles(m, s) * sizeof(double));
+    rc = scr().tsqr.ensure((size_t)tsqr_workspace_doubles(m, s) * sizeof(double));
     if (rc) return rc;
     if (is_split(precision)) {
-        rc = g_ctx.split.ensure((size_t)split_workspace_bytes(m, n, s, g_ctx.num_sms));
+        rc = scr().split.ensure((size_t)split_workspace_bytes(m, n, s, g_ctx.num_sms));
         if (rc) return rc;
     }
     return 0;
@@ -298,12 +310,12 @@ struct Engine {
         const double eb = is_split(precision) ? 2.0 * split_digits() : 8.0;
         ProfScope ps(0, st, 2.0 * m * na * nb, eb * m * (na + nb));
         if (is_split(precision)) {
-            err = launch_gram_split(X, ld, m, na, b0, nb, C, na, g_ctx.split.as<char>(),
-                                    g_ctx.split.bytes, g_ctx.num_sms, st);
+            err = launch_gram_split(X, ld, m, na, b0, nb, C, na, scr().split.as<char>(),
+                                    scr().split.bytes, g_ctx.num_sms, st);
             return;
         }
         int chunks = gram_chunks_fp64(m, na, nb, g_ctx.num_sms);
-        err = launch_gram_fp64(X, ld, m, 0, na, b0, nb, C, na, g_ctx.part.as<double>(), chunks, st);
+        err = launch_gram_fp64(X, ld, m, 0, na, b0, nb, C, na, scr().part.as<double>(), chunks, st);
     }
     // X[:, c0:c0+nc] = (X[:, c0:c0+nc] - X[:, 0:K] S) T^{-1}
     void update(int K, int c0, int nc, const double* S, int lds, const double* T, int ldt) {
@@ -318,8 +330,8 @@ struct Engine {
                                                  : 8.0 * m * (K + 2.0 * nc);
         ProfScope ps(1, st, 2.0 * m * K * nc + (T ? (double)m * nc * nc : 0.0), bytes);
         if (is_split(precision)) {
-            err = launch_update_split(X, ld, m, K, c0, nc, S, lds, T, ldt, g_ctx.split.as<char>(),
-                                      g_ctx.split.bytes, g_ctx.num_sms, st);
+            err = launch_update_split(X, ld, m, K, c0, nc, S, lds, T, ldt, scr().split.as<char>(),
+                                      scr().split.bytes, g_ctx.num_sms, st);
             return;
         }
         err = launch_update_fp64(X, ld, m, 0, K, c0, nc, S, lds, T, ldt, st);
@@ -360,7 +372,7 @@ struct Engine {
         if (err) return;
         host_sync(c0 + nc, c0);
         ProfScope ps(3, st, 6.0 * m * nc * nc, 8.0 * m * nc * 3.0);
-        err = launch_tsqr(X, ld, m, c0, nc, Rout, ldr, g_ctx.tsqr.as<double>(), st);
+        err = launch_tsqr(X, ld, m, c0, nc, Rout, ldr, scr().tsqr.as<double>(), st);
         if (is_split(precision)) split_mark_stale(c0, nc);
     }
 };
@@ -637,12 +649,12 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
     }
     const long long launches0 = g_launch_count;
     Engine e{dX, (i64)ldX, (i64)m, n, s, dR, ldR, precision, st,
-             carve_small(g_ctx.small.as<double>(), n, s), g_ctx.status.as<int>()};
+             carve_small(scr().small.as<double>(), n, s), scr().status.as<int>()};
     e.link = link;
     cudaError_t ce = cudaMemsetAsync(e.status, 0, kStatusWords * sizeof(int), st);
     if (ce != cudaSuccess) e.err = (int)ce;
     if (!e.err && is_split(precision))
-        e.err = split_begin(dX, ldX, m, n, s, split_digits_of(precision), g_ctx.split.as<char>(), g_ctx.split.bytes, g_ctx.num_sms, st);
+        e.err = split_begin(dX, ldX, m, n, s, split_digits_of(precision), scr().split.as<char>(), scr().split.bytes, g_ctx.num_sms, st);
     switch (variant) {
         case ORTH_GB300_BCGSI2P1S:
             if (is_split(precision) && s <= 16) run_lagged_fused(e, true); else run_p1s(e);
@@ -762,6 +774,79 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
 }
 
 }  // namespace
+
+// Split-precision batches: the matrices one after another on `st` through the
+// single-matrix driver (its digit stores are 28 bytes per element, so a whole
+// batch's stores at once would not fit). Workspaces are grown for the largest
+// shapes first, so no allocation happens between matrices. After each matrix its
+// status words (4 ints) and the split kernels' error word go to dstatus[8 b ..]
+// on the device; nothing waits on the host.
+int split_batch_enqueue(int variant, int count, const int* m, const int* n, const int* s, double* const* dX,
+                        const long long* ldX, double* const* dR, const int* ldR, int precision, cudaStream_t st,
+                        int* dstatus, int max_slots) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (init_ctx()) return 3;
+    int S = count < kSlots ? count : kSlots;
+    if (max_slots >= 1 && S > max_slots) S = max_slots;
+    // Longest job (m n^2) first, each to the least loaded slot.
+    std::vector<int> order(count), slot_of(count);
+    for (int b = 0; b < count; ++b) order[b] = b;
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+        const double wa = (double)m[a] * n[a] * n[a], wb = (double)m[b] * n[b] * n[b];
+        return wa > wb || (wa == wb && a < b);
+    });
+    std::vector<double> load(S, 0.0);
+    for (int b : order) {
+        int k = 0;
+        for (int q = 1; q < S; ++q)
+            if (load[q] < load[k]) k = q;
+        slot_of[b] = k;
+        load[k] += (double)m[b] * n[b] * n[b];
+    }
+    int rc = 0;
+    for (int k = 0; k < S && !rc; ++k)
+        if (!g_ctx.slot_stream[k] &&
+            cudaStreamCreateWithFlags(&g_ctx.slot_stream[k], cudaStreamNonBlocking) != cudaSuccess)
+            rc = 3;
+    // Grow every slot's scratch for its largest shapes before anything is enqueued.
+    for (int i = 0; i < count && !rc; ++i) {
+        const int b = order[i];
+        g_slot = slot_of[b];
+        if (reserve(m[b], n[b], s[b], precision)) rc = 3;
+    }
+    cudaEvent_t fork = nullptr;
+    if (!rc && cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) rc = 3;
+    if (!rc && cudaEventRecord(fork, st) != cudaSuccess) rc = 3;
+    for (int k = 0; k < S && !rc; ++k)
+        if (cudaStreamWaitEvent(g_ctx.slot_stream[k], fork, 0) != cudaSuccess) rc = 3;
+    for (int i = 0; i < count && !rc; ++i) {
+        const int b = order[i], k = slot_of[b];
+        g_slot = k;
+        split_select_slot(k);
+        cudaStream_t ss = g_ctx.slot_stream[k];
+        rc = run_device(variant, m[b], n[b], s[b], dX[b], ldX[b], dR[b], ldR[b], precision, ss, nullptr);
+        if (rc) break;
+        cudaError_t ce = cudaMemcpyAsync(dstatus + 8 * (i64)b, scr().status.as<int>(), kStatusWords * sizeof(int),
+                                         cudaMemcpyDeviceToDevice, ss);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(dstatus + 8 * (i64)b + 4, split_error_ptr(), sizeof(int), cudaMemcpyDeviceToDevice, ss);
+        if (ce != cudaSuccess) rc = 3;
+    }
+    // Join: the caller's stream waits for every slot stream.
+    for (int k = 0; k < S; ++k) {
+        cudaEvent_t j = nullptr;
+        if (cudaEventCreateWithFlags(&j, cudaEventDisableTiming) == cudaSuccess) {
+            cudaEventRecord(j, g_ctx.slot_stream[k]);
+            cudaStreamWaitEvent(st, j, 0);
+            cudaEventDestroy(j);
+        }
+    }
+    if (fork) cudaEventDestroy(fork);
+    g_slot = 0;
+    split_select_slot(0);
+    return rc;
+}
+
 }  // namespace bcgs
 
 using namespace bcgs;
@@ -822,15 +907,15 @@ int orth_gb300_gram_dev(int m, int na, int b0, int nb, const double* dX, long lo
     int rc = init_ctx();
     if (rc) return 3;
     if (precision == ORTH_GB300_FP64) {
-        if (g_ctx.part.ensure((size_t)part_doubles(m, n, s, g_ctx.num_sms) * sizeof(double))) return 3;
+        if (scr().part.ensure((size_t)part_doubles(m, n, s, g_ctx.num_sms) * sizeof(double))) return 3;
         const int chunks = gram_chunks_fp64(m, na, nb, g_ctx.num_sms);
-        rc = launch_gram_fp64(dX, ldX, m, 0, na, b0, nb, dC, ldc, g_ctx.part.as<double>(), chunks, st);
+        rc = launch_gram_fp64(dX, ldX, m, 0, na, b0, nb, dC, ldc, scr().part.as<double>(), chunks, st);
     } else {
-        if (g_ctx.split.ensure((size_t)split_workspace_bytes(m, n, s, g_ctx.num_sms))) return 3;
-        rc = split_begin(const_cast<double*>(dX), ldX, m, n, s, split_digits_of(precision), g_ctx.split.as<char>(), g_ctx.split.bytes,
+        if (scr().split.ensure((size_t)split_workspace_bytes(m, n, s, g_ctx.num_sms))) return 3;
+        rc = split_begin(const_cast<double*>(dX), ldX, m, n, s, split_digits_of(precision), scr().split.as<char>(), scr().split.bytes,
                          g_ctx.num_sms, st);
         if (!rc)
-            rc = launch_gram_split(dX, ldX, m, na, b0, nb, dC, ldc, g_ctx.split.as<char>(), g_ctx.split.bytes,
+            rc = launch_gram_split(dX, ldX, m, na, b0, nb, dC, ldc, scr().split.as<char>(), scr().split.bytes,
                                    g_ctx.num_sms, st);
         if (!rc) {
             int w = 0;
@@ -875,10 +960,10 @@ int orth_gb300_accuracy_dev(int m, int n, const double* dX, long long ldX, const
             const i64 v = (i64)gram_chunks_fp64(m, a, GW, g_ctx.num_sms) * a * GW;
             if (v > need) need = v;
         }
-        if (g_ctx.part.ensure((size_t)(need + 1024) * sizeof(double))) return 3;
+        if (scr().part.ensure((size_t)(need + 1024) * sizeof(double))) return 3;
     } else {
-        if (g_ctx.split.ensure((size_t)split_workspace_bytes(m, n, 16, g_ctx.num_sms))) return 3;
-        rc = split_begin(const_cast<double*>(dQ), ldQ, m, n, 16, 7, g_ctx.split.as<char>(), g_ctx.split.bytes,
+        if (scr().split.ensure((size_t)split_workspace_bytes(m, n, 16, g_ctx.num_sms))) return 3;
+        rc = split_begin(const_cast<double*>(dQ), ldQ, m, n, 16, 7, scr().split.as<char>(), scr().split.bytes,
                          g_ctx.num_sms, st);
         if (rc) return 3;
     }
@@ -888,10 +973,10 @@ int orth_gb300_accuracy_dev(int m, int n, const double* dX, long long ldX, const
         const int na = c0 + nb;
         if (gram_precision == ORTH_GB300_FP64) {
             const int chunks = gram_chunks_fp64(m, na, nb, g_ctx.num_sms);
-            rc = launch_gram_fp64(dQ, ldQ, m, 0, na, c0, nb, G + (i64)c0 * n, n, g_ctx.part.as<double>(), chunks, st);
+            rc = launch_gram_fp64(dQ, ldQ, m, 0, na, c0, nb, G + (i64)c0 * n, n, scr().part.as<double>(), chunks, st);
         } else {
-            rc = launch_gram_split(dQ, ldQ, m, na, c0, nb, G + (i64)c0 * n, n, g_ctx.split.as<char>(),
-                                   g_ctx.split.bytes, g_ctx.num_sms, st);
+            rc = launch_gram_split(dQ, ldQ, m, na, c0, nb, G + (i64)c0 * n, n, scr().split.as<char>(),
+                                   scr().split.bytes, g_ctx.num_sms, st);
         }
     }
     if (!rc && gram_precision != ORTH_GB300_FP64) {
@@ -963,14 +1048,18 @@ int orth_gb300_reserve(int m, int n, int s) {
 
 void orth_gb300_release(void) {
     std::lock_guard<std::mutex> lock(g_mu);
-    g_ctx.part.release();
+    for (Scratch& sc : g_scratch) {
+        sc.part.release();
+        sc.small.release();
+        sc.status.release();
+        sc.tsqr.release();
+        sc.split.release();
+    }
+    split_forget_workspaces();
     g_ctx.gram.release();
-    g_ctx.small.release();
-    g_ctx.status.release();
-    g_ctx.tsqr.release();
+    g_ctx.metric.release();
     g_ctx.hostX.release();
     g_ctx.hostR.release();
-    g_ctx.split.release();
     if (g_ctx.hostR_stage) cudaFreeHost(g_ctx.hostR_stage);
     g_ctx.hostR_stage = nullptr;
     g_ctx.hostR_stage_bytes = 0;

@@ -26,6 +26,12 @@ void split_mark_stale(int c0, int nc);
 // Reads (and waits for) the split kernels' error word: 0, or the code of a wait
 // that ran out.
 int split_error_word(int* out, cudaStream_t st);
+// Device address of the error word of the current run (valid after split_begin).
+int* split_error_ptr();
+// Selects the plan (digit stores, maps, freshness) the calls above use: 0 .. 7.
+void split_select_slot(int slot);
+// Forget which workspaces were zeroed (call after freeing them).
+void split_forget_workspaces();
 // Last nonzero error word seen: the code of the bounded wait that ran out (for the
 // A-ring waits, code + 100 * ring slot).
 int split_last_error();

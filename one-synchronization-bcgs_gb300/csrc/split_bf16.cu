@@ -802,7 +802,12 @@ struct Plan {
     i64 zeroed_m = -1;
     int zeroed_n = -1;
 };
-Plan g_plan;
+// One plan per scratch slot (split-precision batches run several at once on
+// separate streams); slot 0 serves every single-matrix entry point.
+constexpr int kPlanSlots = 8;
+Plan g_plans[kPlanSlots];
+int g_plan_slot = 0;
+inline Plan& cur_plan() { return g_plans[g_plan_slot]; }
 
 struct Carve {
     char* p;
@@ -854,7 +859,7 @@ size_t layout_bytes(i64 m, int n, int s, int num_sms, Plan* out, char* base) {
 }
 
 int ensure_fresh(int c_begin, int c_end, cudaStream_t st) {
-    Plan& P = g_plan;
+    Plan& P = cur_plan();
     int c = c_begin;
     while (c < c_end) {
         if (P.fresh[c]) { ++c; continue; }
@@ -897,7 +902,7 @@ i64 split_workspace_bytes(i64 m, int n, int s, int num_sms) {
 
 int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t ws_bytes, int num_sms,
                 cudaStream_t st) {
-    Plan& P = g_plan;
+    Plan& P = cur_plan();
     if (kd != 6 && kd != 7) return (int)cudaErrorInvalidValue;
     P.kd = kd;
     const size_t need = layout_bytes(m, n, s, num_sms, &P, ws);
@@ -944,16 +949,30 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
 }
 
 void split_mark_stale(int c0, int nc) {
-    for (int c = c0; c < c0 + nc && c < (int)g_plan.fresh.size(); ++c) {
-        g_plan.fresh[c] = 0;
-        g_plan.cmax_valid[c] = 0;
+    for (int c = c0; c < c0 + nc && c < (int)cur_plan().fresh.size(); ++c) {
+        cur_plan().fresh[c] = 0;
+        cur_plan().cmax_valid[c] = 0;
     }
 }
+
+// The workspaces were freed: a new one may come back at the same address, so no
+// plan may treat its stores as already zeroed.
+void split_forget_workspaces() {
+    for (Plan& P : g_plans) {
+        P.zeroed_base = nullptr;
+        P.zeroed_m = -1;
+        P.zeroed_n = -1;
+    }
+}
+
+void split_select_slot(int slot) { g_plan_slot = (slot >= 0 && slot < kPlanSlots) ? slot : 0; }
+
+int* split_error_ptr() { return cur_plan().err; }
 
 int g_last_split_error = 0;
 
 int split_error_word(int* out, cudaStream_t st) {
-    cudaError_t ce = cudaMemcpyAsync(out, g_plan.err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaError_t ce = cudaMemcpyAsync(out, cur_plan().err, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce == cudaSuccess && *out) g_last_split_error = *out;
     return (int)ce;
@@ -963,12 +982,12 @@ int split_last_error() { return g_last_split_error; }
 
 int split_prepare(int c_end, cudaStream_t st) { return ensure_fresh(0, c_end, st); }
 
-int split_digits() { return g_plan.kd; }
+int split_digits() { return cur_plan().kd; }
 
 int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, double* out, int ldo,
                       char* ws, size_t ws_bytes, int num_sms, cudaStream_t st) {
     (void)X; (void)ld; (void)ws; (void)ws_bytes;
-    Plan& P = g_plan;
+    Plan& P = cur_plan();
     if (na <= 0 || nb <= 0) return 0;
     int rc = ensure_fresh(0, na > b0 + nb ? na : b0 + nb, st);
     if (rc) return rc;
@@ -1003,7 +1022,7 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
 // group reads the same digit planes of X[:, 0:kin], which were sliced before the
 // first group wrote anything, and its own 32 columns of the factor in Bp.
 static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int num_sms, cudaStream_t st) {
-    Plan& P = g_plan;
+    Plan& P = cur_plan();
     for (int j0 = 0; j0 < nc; j0 += 32) {
         const int ng = nc - j0 < 32 ? nc - j0 : 32;
         const int NB = ng <= 16 ? 16 : 32;
@@ -1041,7 +1060,7 @@ static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int 
 int launch_update_split(double* X, i64 ld, i64 m, int K, int c0, int nc, const double* S, int lds,
                         const double* T, int ldt, char* ws, size_t ws_bytes, int num_sms, cudaStream_t st) {
     (void)ws; (void)ws_bytes;
-    Plan& P = g_plan;
+    Plan& P = cur_plan();
     if (nc <= 0) return 0;
     if (c0 != K || nc > 64 || X != P.X) return (int)cudaErrorInvalidValue;
     int rc = ensure_fresh(0, K + nc, st);
@@ -1058,7 +1077,7 @@ int launch_update_split(double* X, i64 ld, i64 m, int K, int c0, int nc, const d
 int launch_fused_update_split(double* X, i64 ld, i64 m, int K, int s, int nz, const double* G, int ldg,
                               const double* Ty, const double* Sp, int ldsp, const double* Ts, int num_sms,
                               cudaStream_t st) {
-    Plan& P = g_plan;
+    Plan& P = cur_plan();
     const int kin = K + s + nz, nout = s + nz;
     if (s > 16 || nz > 16 || nout > 32 || X != P.X) return (int)cudaErrorInvalidValue;
     int rc = ensure_fresh(0, kin, st);

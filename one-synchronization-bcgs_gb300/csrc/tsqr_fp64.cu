@@ -210,9 +210,11 @@ __device__ void tsqr_apply_body(double* Q, i64 ldq, i64 rows, int nc, int TR, co
     __syncthreads();
     const i64 r = blk * blockDim.x + threadIdx.x;
     const i64 t = (blk * blockDim.x) / TR;   // blockDim.x divides TR
-    for (int e = threadIdx.x; e < nc * nc; e += blockDim.x) {
-        int i = e % nc, c = e / nc;
-        p[i + c * NC] = P[t * nc + i + (i64)c * ldp];
+    // The whole NC x NC tile: the product below runs over NC terms, and entries
+    // past nc must be zeros, not whatever an earlier CTA left in shared memory.
+    for (int e = threadIdx.x; e < NC * NC; e += blockDim.x) {
+        const int i = e % NC, c = e / NC;
+        p[e] = (i < nc && c < nc) ? P[t * nc + i + (i64)c * ldp] : 0.0;
     }
     __syncthreads();
     if (r >= rows) return;   // the last statement of the body: no barrier follows

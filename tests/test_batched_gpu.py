@@ -129,5 +129,44 @@ def test_batch_rejects_bad_arguments(lib):
     r = torch.zeros((32, 32), dtype=torch.float64, device="cuda")
     assert orth.Batch([3000], [32], [32], [x.data_ptr()], [r.data_ptr()]).rc == 2        # s > 16
     assert orth.Batch([3000], [32], [8], [x.data_ptr()], [r.data_ptr()], ldx=[2999]).rc == 2
-    assert orth.Batch([3000], [32], [8], [x.data_ptr()], [r.data_ptr()], precision=orth.SPLIT_BF16).rc == 4
+    assert orth.Batch([3000], [32], [8], [x.data_ptr()], [r.data_ptr()], precision=7).rc == 4
     assert orth.Batch([3000], [32], [8], [x.data_ptr()], [r.data_ptr()], variant="bcgsi2").rc == 4
+
+
+@pytest.mark.parametrize("variant", ["bcgsi2P1s", "bcgsi21s"])
+def test_split_batch_matches_single_split_runs(lib, variant):
+    """Split-precision batches run each matrix through the single-matrix tensor-core
+    driver: bit-identical to orth_gb300_run_dev per matrix, and within 10x of the
+    FP64 path's LOO and residual; breakdowns are reported per matrix."""
+    torch = pytest.importorskip("torch")
+    ms, ns, ss, mats = _batch(seed=21, count=10, m_hi=20000, p_hi=6, kappa_hi=1e6)
+    dX = _to_dev(torch, mats)
+    dR = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for n in ns]
+    st = torch.cuda.current_stream().cuda_stream
+    plan = orth.Batch(ms, ns, ss, [x.data_ptr() for x in dX], [r.data_ptr() for r in dR],
+                      precision=orth.SPLIT_BF16, stream=st, variant=variant)
+    assert plan.rc == 0
+    for rep in range(2):                       # two runs: stores re-zeroed per shape
+        for b, X in enumerate(mats):
+            dX[b].copy_(torch.from_numpy(np.ascontiguousarray(X.T)))
+            dR[b].zero_()
+        assert plan.run(st) == 0
+        rc, steps, _, _ = plan.status()
+        assert rc == 0
+    for b, X in enumerate(mats):
+        m, n, s = ms[b], ns[b], ss[b]
+        outs = {}
+        for prec in (orth.SPLIT_BF16, orth.FP64):
+            x1 = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
+            r1 = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+            rc1, st1 = orth.run_dev(variant, m, n, s, x1.data_ptr(), m, r1.data_ptr(), n, prec, st)
+            assert rc1 == 0
+            outs[prec] = (x1.cpu().numpy().T, r1.cpu().numpy().T, st1["breakdown_step"])
+        Qs, Rs, step_s = outs[orth.SPLIT_BF16]
+        assert np.array_equal(dX[b].cpu().numpy().T, Qs) and np.array_equal(dR[b].cpu().numpy().T, Rs), b
+        assert steps[b] == step_s
+        Qf, Rf, _ = outs[orth.FP64]
+        if step_s == 0:
+            assert port.loo_2(Qs) <= 10 * max(port.loo_2(Qf), 1e-15)
+            assert port.rel_residual(X, Qs, np.triu(Rs)) <= 10 * max(port.rel_residual(X, Qf, np.triu(Rf)), 1e-15)
+    plan.close()
