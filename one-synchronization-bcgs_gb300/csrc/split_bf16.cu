@@ -442,16 +442,37 @@ __device__ __forceinline__ double assemble(long long hi, long long mid, float lo
 template <int NB, int KD, class CoordFn>
 __device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapA, const CUtensorMap* mapB, uint8_t* sA,
                                               uint8_t* sB, Bars* bars, Ring& ra, Ring& rb, CoordFn coords,
-                                              int item, int ch, volatile int* abort, int* err) {
+                                              int item, int ch, volatile int* abort, int* err, int cs = 1,
+                                              int rank = 0) {
     constexpr int B_SLOT = SmemLayout<NB, KD>::B_SLOT;
     // Plane p of A is at (ax, ay, az + p*azs); plane p of B at (bx, by, bz + p*bzs).
     int ax, ay, az, azs, bx, by, bz, bzs;
     coords(item, ch, ax, ay, az, azs, bx, by, bz, bzs);
-    if (!tc::mbar_wait(&bars->b_empty[rb.slot], rb.phase ^ 1u, abort, err, 11)) return false;
-    tc::mbar_expect_tx(&bars->b_full[rb.slot], (uint32_t)B_SLOT);
+    if (cs == 1) {
+        if (!tc::mbar_wait(&bars->b_empty[rb.slot], rb.phase ^ 1u, abort, err, 11)) return false;
+        tc::mbar_expect_tx(&bars->b_full[rb.slot], (uint32_t)B_SLOT);
 #pragma unroll
-    for (int j = 0; j < KD; ++j)
-        tc::tma_load_3d(sB + rb.slot * B_SLOT + j * NB * KCH * 2, mapB, &bars->b_full[rb.slot], bx, by, bz + j * bzs);
+        for (int j = 0; j < KD; ++j)
+            tc::tma_load_3d(sB + rb.slot * B_SLOT + j * NB * KCH * 2, mapB, &bars->b_full[rb.slot], bx, by,
+                            bz + j * bzs);
+    } else if (rank == 0) {
+        // Cluster leader: the B slot is free in every CTA once all cs MMA threads
+        // released it (remote arrivals on this CTA's b_empty); one multicast load
+        // fills it everywhere.
+        if (!tc::mbar_wait(&bars->b_empty[rb.slot], rb.phase ^ 1u, abort, err, 13)) return false;
+        tc::mbar_expect_tx(&bars->b_full[rb.slot], (uint32_t)B_SLOT);
+        const uint16_t mask = (uint16_t)((1u << cs) - 1u);
+#pragma unroll
+        for (int j = 0; j < KD; ++j)
+            tc::tma_load_3d_mc(sB + rb.slot * B_SLOT + j * NB * KCH * 2, mapB, &bars->b_full[rb.slot], bx, by,
+                               bz + j * bzs, mask);
+    } else {
+        // Other CTAs only arm their own b_full for the bytes the leader sends, once
+        // the previous use of the slot has completed here (no second arrival may
+        // fall into a phase that is still open).
+        if (!tc::mbar_wait(&bars->b_full[rb.slot], rb.phase ^ 1u, abort, err, 14)) return false;
+        tc::mbar_expect_tx(&bars->b_full[rb.slot], (uint32_t)B_SLOT);
+    }
     rb.advance(RB);
 #pragma unroll
     for (int i = 0; i < KD; ++i) {
@@ -467,7 +488,7 @@ __device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapA, const CUt
 template <int NB, int KD>
 __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uint8_t* sA, uint8_t* sB,
                                           Bars* bars, Ring& ra, Ring& rb, bool first_in_window,
-                                          volatile int* abort, int* err) {
+                                          volatile int* abort, int* err, int cs = 1) {
     constexpr int B_SLOT = SmemLayout<NB, KD>::B_SLOT;
     if (!tc::mbar_wait(&bars->b_full[rb.slot], rb.phase, abort, err, 21)) return false;
     const uint32_t b_addr = tc::smem_u32(sB + rb.slot * B_SLOT);
@@ -487,13 +508,15 @@ __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uin
         tc::mma_commit(&bars->a_empty[ra.slot]);
         ra.advance(RA);
     }
-    tc::mma_commit(&bars->b_empty[rb.slot]);
+    if (cs == 1) tc::mma_commit(&bars->b_empty[rb.slot]);
+    else tc::mma_commit_mc(&bars->b_empty[rb.slot], (uint16_t)1u);   // release to the cluster leader
     rb.advance(RB);
     return true;
 }
 
 template <int NB, int KD>
-__device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint8_t*& sB, uint32_t* tmem_slot) {
+__device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint8_t*& sB, uint32_t* tmem_slot,
+                                           int cs = 1) {
     using L = SmemLayout<NB, KD>;
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     sA = base + L::A_OFF;
@@ -502,7 +525,8 @@ __device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint
     const int warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         for (int i = 0; i < RA; ++i) { tc::mbar_init(&bars->a_full[i], 1); tc::mbar_init(&bars->a_empty[i], 1); }
-        for (int i = 0; i < RB; ++i) { tc::mbar_init(&bars->b_full[i], 1); tc::mbar_init(&bars->b_empty[i], 1); }
+        // b_empty counts one release per CTA of the cluster (cs = 1: no cluster).
+        for (int i = 0; i < RB; ++i) { tc::mbar_init(&bars->b_full[i], 1); tc::mbar_init(&bars->b_empty[i], (uint32_t)cs); }
         for (int i = 0; i < 2; ++i) { tc::mbar_init(&bars->t_full[i], 1); tc::mbar_init(&bars->t_empty[i], NEPI); }
         tc::mbar_init(&bars->drain, 1);
         tc::fence_mbar_init();
@@ -520,6 +544,7 @@ __device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint
 // ---------------------------------------------------------------------------
 struct GramParams {
     int na, nb, b0, nrc;
+    int cs;          // cluster size: the numMB CTAs of one (row range, N-group) share B by multicast
     i64 m;
     int numMB, numNG, rc;
     i64 rows_per;   // multiple of WIN*KCH
@@ -538,7 +563,10 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     __shared__ volatile int abort_flag;
     uint8_t *sA, *sB;
     if (threadIdx.x == 0) abort_flag = 0;
-    Bars* bars = setup_cta<NB, KD>(smem_raw, sA, sB, &tmem_slot);
+    const int cs = p.cs;
+    Bars* bars = setup_cta<NB, KD>(smem_raw, sA, sB, &tmem_slot, cs);
+    const int rank = cs > 1 ? (int)tc::cluster_rank() : 0;
+    if (cs > 1) tc::cluster_sync();   // peers' barriers are initialized before any remote arrive
     const uint32_t tmem = tmem_slot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -561,7 +589,9 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
         if (lane == 0) {
             Ring ra, rb;
             for (int ch = 0; ch < nchunks; ++ch)
-                if (!produce_chunk<NB, KD>(&mapA, &mapB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag, p.err)) break;
+                if (!produce_chunk<NB, KD>(&mapA, &mapB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag, p.err, cs,
+                                           rank))
+                    break;
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -575,7 +605,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
                 const int c_end = min(nchunks, (w + 1) * WIN);
                 for (int ch = w * WIN; ch < c_end && ok; ++ch)
                     ok = mma_chunk<NB, KD>(tmem, (uint32_t)(buf * L::TMEM_COLS_PER_BUF), sA, sB, bars, ra, rb,
-                                       ch == w * WIN, &abort_flag, p.err);
+                                       ch == w * WIN, &abort_flag, p.err, cs);
                 if (ok) tc::mma_commit(&bars->t_full[buf]);
             }
             tc::mma_commit(&bars->drain);
@@ -617,9 +647,15 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     }
     __syncthreads();
     if (warp == 1) {
-        // All MMAs issued by this CTA have completed once `drain` fires.
+        // All MMAs issued by this CTA have completed once `drain` fires (then its
+        // last remote releases have reached the leader too).
         if (lane == 0) tc::mbar_wait(&bars->drain, 0, &abort_flag, p.err, 51);
         __syncwarp();
+    }
+    // No CTA leaves while a peer may still arrive on its barriers or receive its
+    // multicast; every CTA reaches this point, also after a wait gave up.
+    if (cs > 1) tc::cluster_sync();
+    if (warp == 1) {
         tc::tc_fence_after();
         tc::tmem_dealloc(tmem, (uint32_t)L::TMEM_ALLOC);
     }
@@ -1004,12 +1040,52 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     gp.part = P.part;
     gp.err = P.err;
     if ((i64)gp.rc * na * nb > P.part_doubles) return (int)cudaErrorInvalidValue;
-    if (P.kd == 6)
-        gram_tc_kernel<6><<<(unsigned)(mbn * gp.rc), NTHREADS, SmemLayout<32, 6>::BYTES, st>>>(P.map_col_a,
-                                                                                              P.map_col_b, gp);
-    else
-        gram_tc_kernel<7><<<(unsigned)(mbn * gp.rc), NTHREADS, SmemLayout<32, 7>::BYTES, st>>>(P.map_col_a,
-                                                                                              P.map_col_b, gp);
+    // The numMB CTAs of one (row range, N-group) are consecutive in blockIdx.x; as a
+    // cluster they read each B tile once (multicast) instead of numMB times.
+    gp.cs = (gp.numMB > 1 && gp.numMB <= 8) ? gp.numMB : 1;
+    cudaLaunchConfig_t cfg = {};
+    if (gp.cs > 1) {
+        // Clusters must sit whole inside a GPC: take only as many row ranges as can
+        // run at once, so that the launch is a single wave of clusters.
+        cudaLaunchConfig_t q = {};
+        cudaLaunchAttribute qa[1];
+        q.gridDim = dim3((unsigned)(mbn * gp.rc));
+        q.blockDim = dim3(NTHREADS);
+        q.dynamicSmemBytes = P.kd == 6 ? SmemLayout<32, 6>::BYTES : SmemLayout<32, 7>::BYTES;
+        qa[0].id = cudaLaunchAttributeClusterDimension;
+        qa[0].val.clusterDim.x = (unsigned)gp.cs;
+        qa[0].val.clusterDim.y = 1;
+        qa[0].val.clusterDim.z = 1;
+        q.attrs = qa;
+        q.numAttrs = 1;
+        int maxc = 0;
+        cudaError_t oe = P.kd == 6 ? cudaOccupancyMaxActiveClusters(&maxc, gram_tc_kernel<6>, &q)
+                                   : cudaOccupancyMaxActiveClusters(&maxc, gram_tc_kernel<7>, &q);
+        if (oe == cudaSuccess && maxc > 0) {
+            const int rc_fit = maxc / gp.numNG > 0 ? maxc / gp.numNG : 1;
+            if (rc_fit < gp.rc) {
+                gp.rows_per = round_up(ceil_div(m, rc_fit), (i64)WIN * KCH);
+                gp.rc = (int)ceil_div(m, gp.rows_per);
+            }
+        } else {
+            (void)cudaGetLastError();
+            gp.cs = 1;
+        }
+    }
+    cudaLaunchAttribute attr[1];
+    cfg.gridDim = dim3((unsigned)(mbn * gp.rc));
+    cfg.blockDim = dim3(NTHREADS);
+    cfg.dynamicSmemBytes = P.kd == 6 ? SmemLayout<32, 6>::BYTES : SmemLayout<32, 7>::BYTES;
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)gp.cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t lce = P.kd == 6 ? cudaLaunchKernelEx(&cfg, gram_tc_kernel<6>, P.map_col_a, P.map_col_b, gp)
+                                : cudaLaunchKernelEx(&cfg, gram_tc_kernel<7>, P.map_col_a, P.map_col_b, gp);
+    if (lce != cudaSuccess) return (int)lce;
     g_launch_count += 1;
     rc = (int)cudaGetLastError();
     if (rc) return rc;
