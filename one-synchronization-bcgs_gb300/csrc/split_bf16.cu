@@ -370,14 +370,17 @@ struct SmemLayout {
     static constexpr int A_OFF = 0;
     static constexpr int B_OFF = RA * A_SLOT;
     static constexpr int BAR_OFF = B_OFF + RB * B_SLOT;
-    static constexpr int BYTES = BAR_OFF + 256 + 1024;  // barriers + alignment slack
+    static constexpr int BYTES = BAR_OFF + 512 + 1024;  // barriers (<= 512 B) + alignment slack
     static constexpr int TMEM_COLS_PER_BUF = NB * KD;
     static constexpr int TMEM_ALLOC = (2 * TMEM_COLS_PER_BUF) <= 128 ? 128 : ((2 * TMEM_COLS_PER_BUF) <= 256 ? 256 : 512);
 };
 
+constexpr int RQ = 4;          // tile-number ring depth (update kernel)
 struct Bars {
     uint64_t a_full[RA], a_empty[RA], b_full[RB], b_empty[RB], t_full[2], t_empty[2], drain;
+    uint64_t q_full[RQ], q_empty[RQ];
 };
+static_assert(sizeof(Bars) <= 512, "barrier block exceeds its shared-memory reservation");
 
 // Per-window epilogue accumulation of the TMEM groups: groups 0-2 (weights 1,
 // 2^-8, 2^-16) into the exact 64-bit integer hi, groups 3-5 into the exact 64-bit
@@ -529,6 +532,8 @@ __device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint
         for (int i = 0; i < RB; ++i) { tc::mbar_init(&bars->b_full[i], 1); tc::mbar_init(&bars->b_empty[i], (uint32_t)cs); }
         for (int i = 0; i < 2; ++i) { tc::mbar_init(&bars->t_full[i], 1); tc::mbar_init(&bars->t_empty[i], NEPI); }
         tc::mbar_init(&bars->drain, 1);
+        // Tile-number ring: one producer; the MMA thread and the 8 epilogue warps read.
+        for (int i = 0; i < RQ; ++i) { tc::mbar_init(&bars->q_full[i], 1); tc::mbar_init(&bars->q_empty[i], 1 + NEPI / 32); }
         tc::fence_mbar_init();
     }
     if (warp == 1) tc::tmem_alloc(tmem_slot, (uint32_t)L::TMEM_ALLOC);
@@ -675,6 +680,7 @@ struct UpdateParams {
     const int* fexp;
     unsigned long long* cmax;   // column max |X[:, c0 + j]| of the written block (bit patterns)
     int* err;
+    int* tile_ctr;              // zeroed before the launch; CTAs take row tiles from it
 };
 
 template <int NB, int KD>
@@ -702,20 +708,38 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
         bx = ch * KCH; by = 0; bz = 0; bzs = 1;
     };
 
+    // Row tiles are handed out dynamically: the producer takes the next tile number
+    // from the launch's counter and publishes it through the ring s_tile/q_*; the
+    // MMA thread and every epilogue warp read the same sequence. A number >= ntiles
+    // ends all three loops. Each tile's arithmetic does not depend on which CTA
+    // runs it.
+    __shared__ int s_tile[RQ];
     if (warp == 0) {
         if (lane == 0) {
-            Ring ra, rb;
+            Ring ra, rb, rq;
             bool ok = true;
-            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x)
+            while (ok) {
+                const int tile = atomicAdd(p.tile_ctr, 1);
+                if (!tc::mbar_wait(&bars->q_empty[rq.slot], rq.phase ^ 1u, &abort_flag, p.err, 15)) break;
+                s_tile[rq.slot] = tile;
+                tc::mbar_arrive(&bars->q_full[rq.slot]);
+                rq.advance(RQ);
+                if (tile >= ntiles) break;
                 for (int ch = 0; ch < nchunks && ok; ++ch)
                     ok = produce_chunk<NB, KD>(&mapA, &mapB, sA, sB, bars, ra, rb, coords, tile, ch, &abort_flag, p.err);
+            }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            Ring ra, rb;
+            Ring ra, rb, rq;
             bool ok = true;
             int wc = 0;  // window counter across tiles
-            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+            while (ok) {
+                if (!tc::mbar_wait(&bars->q_full[rq.slot], rq.phase, &abort_flag, p.err, 33)) break;
+                const int tile = s_tile[rq.slot];
+                tc::mbar_arrive(&bars->q_empty[rq.slot]);
+                rq.advance(RQ);
+                if (tile >= ntiles) break;
                 for (int w = 0; w < nwin && ok; ++w, ++wc) {
                     const int buf = wc & 1;
                     const uint32_t tph = (uint32_t)((wc >> 1) & 1);
@@ -737,7 +761,19 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
         const int rloc = quarter * 32 + lane;
         int wc = 0;
         bool ok = true;
-        for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        Ring rq;
+        while (ok) {
+            int tile = 0;
+            if (lane == 0) {
+                if (!tc::mbar_wait(&bars->q_full[rq.slot], rq.phase, &abort_flag, p.err, 43)) tile = -1;
+                else tile = s_tile[rq.slot];
+            }
+            tile = __shfl_sync(0xffffffffu, tile, 0);
+            if (tile < 0) break;
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&bars->q_empty[rq.slot]);
+            rq.advance(RQ);
+            if (tile >= ntiles) break;
             long long hi[NH], mid[NH];
             float lo[NH];
 #pragma unroll
@@ -825,7 +861,7 @@ struct Plan {
     i64 nrc = 0, ncc = 0, kpad = 0;   // 64-row chunks (column store), 64-column chunks (row store)
     // device buffers (carved from the workspace)
     unsigned short *colstore = nullptr, *rowstore = nullptr, *bdig = nullptr;
-    int *cexp = nullptr, *fexp = nullptr, *err = nullptr;
+    int *cexp = nullptr, *fexp = nullptr, *err = nullptr, *tile_ctr = nullptr;
     unsigned long long *cmax = nullptr, *bmax = nullptr;
     double *bfull = nullptr, *part = nullptr;
     i64 part_doubles = 0;
@@ -879,6 +915,7 @@ size_t layout_bytes(i64 m, int n, int s, int num_sms, Plan* out, char* base) {
     int* cexp = cv.take<int>(n + 64);
     int* fexp = cv.take<int>(64);
     int* err = cv.take<int>(16);
+    int* tctr = cv.take<int>(16);
     unsigned long long* cmax = cv.take<unsigned long long>(n + 64);
     unsigned long long* bmax = cv.take<unsigned long long>(64);
     double* bfull = cv.take<double>(kpad * 64);
@@ -887,7 +924,7 @@ size_t layout_bytes(i64 m, int n, int s, int num_sms, Plan* out, char* base) {
     if (out) {
         out->nrc = nrc; out->ncc = ncc; out->kpad = kpad;
         out->colstore = col; out->rowstore = row; out->bdig = bd;
-        out->cexp = cexp; out->fexp = fexp; out->err = err;
+        out->cexp = cexp; out->fexp = fexp; out->err = err; out->tile_ctr = tctr;
         out->cmax = cmax; out->bmax = bmax; out->bfull = bfull; out->part = part;
         out->part_doubles = pd;
     }
@@ -1116,7 +1153,9 @@ static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int 
         UpdateParams up;
         up.ncc = (int)P.ncc;
         up.m = m; up.kin = kin; up.nc = ng; up.c0 = c0 + j0; up.ld = ld; up.X = X; up.fexp = P.fexp;
-        up.cmax = P.cmax; up.err = P.err;
+        up.cmax = P.cmax; up.err = P.err; up.tile_ctr = P.tile_ctr;
+        ce = cudaMemsetAsync(P.tile_ctr, 0, sizeof(int), st);
+        if (ce != cudaSuccess) return (int)ce;
         const int ntiles = (int)ceil_div(m, TILE_M);
         const int grid = ntiles < num_sms ? ntiles : num_sms;
 #define BCGS_UPD(NBT, KDT) \
