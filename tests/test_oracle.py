@@ -84,3 +84,20 @@ def test_monomial_generator_blocks():
     assert np.allclose(np.linalg.norm(X, axis=0), 1.0)
     # Block 2 starts from the last column of block 1.
     assert np.allclose(X[:, 8], X[:, 7])
+
+
+def test_port_matches_reference_at_config0():
+    """The restated oracle against the reference's own results at its CPU-runnable
+    configuration (tests/golden/config0_ref.npz, made by make_config0.py)."""
+    import os
+    from bcgs_gb300 import inputs
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "config0_ref.npz"))
+    m, n, s, kappa, seed = int(g["m"]), int(g["n"]), int(g["s"]), float(g["kappa"]), int(g["seed"])
+    X = inputs.graded_host(m, n, kappa, seed=seed)
+    for v in ("bcgsi2", "bcgsi2P1s"):
+        Q, R, info = port.run_variant(v, X, n, s)
+        R = np.triu(R)
+        Rref = g[f"{v}/R"]
+        sign = np.sign(np.diag(R)) * np.sign(np.diag(Rref))
+        assert np.max(np.abs(sign[:, None] * R - Rref)) <= qr_tolerance(kappa) * np.max(np.abs(Rref))
+        assert port.loo_2(Q) <= 10 * max(float(g[f"{v}/loo_2"]), 1e-15)
