@@ -657,10 +657,10 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
         e.err = split_begin(dX, ldX, m, n, s, split_digits_of(precision), scr().split.as<char>(), scr().split.bytes, g_ctx.num_sms, st);
     switch (variant) {
         case ORTH_GB300_BCGSI2P1S:
-            if (is_split(precision) && s <= 16) run_lagged_fused(e, true); else run_p1s(e);
+            if (is_split(precision)) run_lagged_fused(e, true); else run_p1s(e);
             break;
         case ORTH_GB300_BCGSI21S:
-            if (is_split(precision) && s <= 16) run_lagged_fused(e, false); else run_21s(e);
+            if (is_split(precision)) run_lagged_fused(e, false); else run_21s(e);
             break;
         case ORTH_GB300_BCGSPIPI2: run_pipi(e); break;
         case ORTH_GB300_BCGSI2: run_bcgsi2(e); break;

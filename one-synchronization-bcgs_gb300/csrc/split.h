@@ -43,7 +43,7 @@ int launch_update_split(double* X, i64 ld, i64 m, int K, int c0, int nc, const d
                         const double* T, int ldt, char* ws, size_t ws_bytes, int num_sms,
                         cudaStream_t st);
 
-// Fused update of the lagged one-sync variants (s, nz <= 16), in one product over
+// Fused update of the lagged one-sync variants (s, nz <= 64), in one product over
 // X[:, 0:K+s+nz]: X[:, K:K+s] = (U_k - Q Y) Ty^{-1} (Y = G[0:K, 0:s]) and
 // X[:, K+s:K+s+nz] = (X_{k+1} - [Q Q_k] S') Ts^{-1} (S' = Sp, K+s rows; Ts may be null).
 int launch_fused_update_split(double* X, i64 ld, i64 m, int K, int s, int nz, const double* G, int ldg,

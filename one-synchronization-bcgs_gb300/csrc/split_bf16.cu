@@ -266,25 +266,34 @@ bbuild_fused_kernel(const double* __restrict__ G, int ldg, int K, int s, const d
                     int ldty, const double* __restrict__ Sp, int ldsp, const double* __restrict__ Ts,
                     int ldts, int nz, const int* __restrict__ cexp, double* __restrict__ Bp, int ldb,
                     unsigned long long* __restrict__ bmax) {
-    __shared__ double w1[16][17], w2[16][17], mm[16][17];
+    // Ty^{-1} (s x s), Ts^{-1} (nz x nz) and M (s x nz) in dynamic shared memory,
+    // row stride FW = 65 (s, nz <= 64).
+    constexpr int FW = 65;
+    extern __shared__ double fsm[];
+    double* w1 = fsm;
+    double* w2 = fsm + 64 * FW;
+    double* mm = fsm + 2 * 64 * FW;
+#define W1(i, j) w1[(i) * FW + (j)]
+#define W2(i, j) w2[(i) * FW + (j)]
+#define MM(i, j) mm[(i) * FW + (j)]
     const int tid = threadIdx.x;
-    // Ty^{-1} and Ts^{-1} (upper), one column per thread.
+    // Ty^{-1} and Ts^{-1} (upper), one column per thread (threads 0..63 and 64..127).
     if (tid < s) {
         const int j = tid;
         for (int i = s - 1; i >= 0; --i) {
             double v = (i == j) ? 1.0 : 0.0;
-            for (int l = i + 1; l <= j; ++l) v -= Ty[i + (i64)l * ldty] * w1[l][j];
-            w1[i][j] = (i <= j) ? v / Ty[i + (i64)i * ldty] : 0.0;
+            for (int l = i + 1; l <= j; ++l) v -= Ty[i + (i64)l * ldty] * W1(l, j);
+            W1(i, j) = (i <= j) ? v / Ty[i + (i64)i * ldty] : 0.0;
         }
-    } else if (tid >= 32 && tid < 32 + nz) {
-        const int j = tid - 32;
+    } else if (tid >= 64 && tid < 64 + nz) {
+        const int j = tid - 64;
         for (int i = nz - 1; i >= 0; --i) {
             double v = (i == j) ? 1.0 : 0.0;
             if (Ts != nullptr) {
-                for (int l = i + 1; l <= j; ++l) v -= Ts[i + (i64)l * ldts] * w2[l][j];
-                w2[i][j] = (i <= j) ? v / Ts[i + (i64)i * ldts] : 0.0;
+                for (int l = i + 1; l <= j; ++l) v -= Ts[i + (i64)l * ldts] * W2(l, j);
+                W2(i, j) = (i <= j) ? v / Ts[i + (i64)i * ldts] : 0.0;
             } else {
-                w2[i][j] = v;
+                W2(i, j) = v;
             }
         }
     }
@@ -293,8 +302,8 @@ bbuild_fused_kernel(const double* __restrict__ G, int ldg, int K, int s, const d
     for (int e = tid; e < s * nz; e += blockDim.x) {
         const int a = e % s, l = e / s;
         double v = 0.0;
-        for (int b = a; b < s; ++b) v += w1[a][b] * Sp[(K + b) + (i64)l * ldsp];
-        mm[a][l] = v;
+        for (int b = a; b < s; ++b) v += W1(a, b) * Sp[(K + b) + (i64)l * ldsp];
+        MM(a, l) = v;
     }
     __syncthreads();
     const int kin = K + s + nz, nout = s + nz;
@@ -304,22 +313,22 @@ bbuild_fused_kernel(const double* __restrict__ G, int ldg, int K, int s, const d
         double v = 0.0;
         if (j < s) {
             if (c < K) {
-                for (int l = 0; l <= j; ++l) v -= G[c + (i64)l * ldg] * w1[l][j];
+                for (int l = 0; l <= j; ++l) v -= G[c + (i64)l * ldg] * W1(l, j);
             } else if (c < K + s) {
-                v = w1[c - K][j];
+                v = W1(c - K, j);
             }
         } else {
             const int l = j - s;
             if (c < K) {
                 for (int q = 0; q <= l; ++q) {
                     double tq = -Sp[c + (i64)q * ldsp];
-                    for (int a = 0; a < s; ++a) tq += G[c + (i64)a * ldg] * mm[a][q];
-                    v += tq * w2[q][l];
+                    for (int a = 0; a < s; ++a) tq += G[c + (i64)a * ldg] * MM(a, q);
+                    v += tq * W2(q, l);
                 }
             } else if (c < K + s) {
-                for (int q = 0; q <= l; ++q) v -= mm[c - K][q] * w2[q][l];
+                for (int q = 0; q <= l; ++q) v -= MM(c - K, q) * W2(q, l);
             } else {
-                v = w2[c - K - s][l];
+                v = W2(c - K - s, l);
             }
         }
         v = ldexp(v, cexp[c]);
@@ -329,6 +338,10 @@ bbuild_fused_kernel(const double* __restrict__ G, int ldg, int K, int s, const d
         atomicMax(bmax + j, b);
     }
 }
+
+#undef W1
+#undef W2
+#undef MM
 
 // Digits of the right-hand factor: bdig[plane][j][c] (K-major), zero padded to
 // (NB rows, Kpad columns); fexp[j] = its column scale exponent.
@@ -917,8 +930,8 @@ size_t layout_bytes(i64 m, int n, int s, int num_sms, Plan* out, char* base) {
     int* err = cv.take<int>(16);
     int* tctr = cv.take<int>(16);
     unsigned long long* cmax = cv.take<unsigned long long>(n + 64);
-    unsigned long long* bmax = cv.take<unsigned long long>(64);
-    double* bfull = cv.take<double>(kpad * 64);
+    unsigned long long* bmax = cv.take<unsigned long long>(128);
+    double* bfull = cv.take<double>(kpad * 128);
     const i64 pd = gram_part_doubles(m, n, s, num_sms);
     double* part = cv.take<double>(pd);
     if (out) {
@@ -1194,12 +1207,19 @@ int launch_fused_update_split(double* X, i64 ld, i64 m, int K, int s, int nz, co
                               cudaStream_t st) {
     Plan& P = cur_plan();
     const int kin = K + s + nz, nout = s + nz;
-    if (s > 16 || nz > 16 || nout > 32 || X != P.X) return (int)cudaErrorInvalidValue;
+    if (s > 64 || nz > 64 || X != P.X) return (int)cudaErrorInvalidValue;
     int rc = ensure_fresh(0, kin, st);
     if (rc) return rc;
-    cudaError_t ce = cudaMemsetAsync(P.bmax, 0, 64 * sizeof(unsigned long long), st);
+    cudaError_t ce = cudaMemsetAsync(P.bmax, 0, 128 * sizeof(unsigned long long), st);
     if (ce != cudaSuccess) return (int)ce;
-    bbuild_fused_kernel<<<(unsigned)ceil_div(kin, 64), 256, 0, st>>>(G, ldg, K, s, Ty, s, Sp, ldsp, Ts, nz, nz,
+    static bool fattr = false;
+    if (!fattr) {
+        ce = cudaFuncSetAttribute(bbuild_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(3 * 64 * 65 * sizeof(double)));
+        if (ce != cudaSuccess) return (int)ce;
+        fattr = true;
+    }
+    bbuild_fused_kernel<<<(unsigned)ceil_div(kin, 64), 256, 3 * 64 * 65 * sizeof(double), st>>>(G, ldg, K, s, Ty, s, Sp, ldsp, Ts, nz, nz,
                                                                         P.cexp, P.bfull, (int)P.kpad, P.bmax);
     g_launch_count += 1;
     return finish_update(X, ld, m, kin, K, nout, num_sms, st);
