@@ -313,14 +313,8 @@ def run_ours(args, rank, world, local_rank):
         ms_ = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
         return ms_, ({} if args.no_accuracy else accuracy())
 
-    # FP64 leg and 48-bit split leg beside the 56-bit split run.
-    fp64_ms = fp64_acc = fast_ms = fast_acc = None
-    if prec != orth.FP64 and args.fp64_steps > 0:
-        fp64_ms, fp64_acc = side_leg(orth.FP64, args.fp64_steps)
-    if prec != orth.FP64 and args.fast_steps > 0:
-        fast_ms, fast_acc = side_leg(orth.SPLIT_BF16_FAST, args.fast_steps)
-
-    # End to end through the orth.h host entry point (pinned host buffers).
+    # End to end through the orth.h host entry point (pinned host buffers), right after
+    # the timed region, before the side legs change the GPU's state.
     e2e = None
     if not args.no_e2e and args.e2e_steps > 0:
         import numpy as np
@@ -347,6 +341,13 @@ def run_ours(args, rank, world, local_rank):
                "h2d_bytes_per_step": m * n * 8, "d2h_bytes_per_step": m * n * 8 + n * n * 8,
                "path": f"orth.h {variant} (host pointers, pinned), {prec_name}"}
         del Xh_t, Rh_t
+
+    # FP64 leg and 48-bit split leg beside the 56-bit split run.
+    fp64_ms = fp64_acc = fast_ms = fast_acc = None
+    if prec != orth.FP64 and args.fp64_steps > 0:
+        fp64_ms, fp64_acc = side_leg(orth.FP64, args.fp64_steps)
+    if prec != orth.FP64 and args.fast_steps > 0:
+        fast_ms, fast_acc = side_leg(orth.SPLIT_BF16_FAST, args.fast_steps)
 
     # Roofline of the dominant kernel class.
     dom = max(("gram", "update"), key=lambda c: prof[c]["ms"])
