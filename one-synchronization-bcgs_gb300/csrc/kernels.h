@@ -3,14 +3,17 @@
 // `st` and returns a cudaError_t value (0 on success).
 #pragma once
 
+#include <atomic>
+
 #include <cuda_runtime.h>
 
 namespace bcgs {
 
 using i64 = long long;
 
-// Number of kernels enqueued by the launchers below since load (host counter).
-extern long long g_launch_count;
+// Number of kernels enqueued by the launchers below since load (host counter;
+// split-precision batches enqueue from several host threads).
+extern std::atomic<long long> g_launch_count;
 
 // C (na x nb, ld ldo) = X[:, a0:a0+na]^T X[:, b0:b0+nb] over m rows, FP64, with a
 // fixed-order two-stage reduction through `part` (nchunks * na * nb doubles).

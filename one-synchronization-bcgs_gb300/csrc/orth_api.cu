@@ -21,7 +21,7 @@
 
 namespace bcgs {
 
-long long g_launch_count = 0;
+std::atomic<long long> g_launch_count{0};
 
 static inline bool is_split(int precision) {
     return precision == ORTH_GB300_SPLIT_BF16 || precision == ORTH_GB300_SPLIT_BF16_FAST;
@@ -61,7 +61,7 @@ struct Scratch {
     DevBuf part, small, status, tsqr, split;
 };
 Scratch g_scratch[kSlots];
-int g_slot = 0;
+thread_local int g_slot = 0;
 inline Scratch& scr() { return g_scratch[g_slot]; }
 
 struct Context {
@@ -138,7 +138,7 @@ int host_precision() {
     }
     return g_host_precision;
 }
-long long g_last_launches = 0;
+std::atomic<long long> g_last_launches{0};
 
 int init_ctx() {
     if (g_ctx.init) return 0;
@@ -832,6 +832,8 @@ int split_batch_enqueue(int variant, int count, const int* m, const int* n, cons
             ce = cudaMemcpyAsync(dstatus + 8 * (i64)b + 4, split_error_ptr(), sizeof(int), cudaMemcpyDeviceToDevice, ss);
         if (ce != cudaSuccess) rc = 3;
     }
+    g_slot = 0;
+    split_select_slot(0);
     // Join: the caller's stream waits for every slot stream.
     for (int k = 0; k < S; ++k) {
         cudaEvent_t j = nullptr;
@@ -842,8 +844,6 @@ int split_batch_enqueue(int variant, int count, const int* m, const int* n, cons
         }
     }
     if (fork) cudaEventDestroy(fork);
-    g_slot = 0;
-    split_select_slot(0);
     return rc;
 }
 

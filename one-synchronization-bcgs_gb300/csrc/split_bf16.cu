@@ -837,15 +837,15 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
 // Host side: workspace plan, tensor maps, digit freshness.
 // ---------------------------------------------------------------------------
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {   // once, thread-safe
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
+            return (PFN_cuTensorMapEncodeTiled_v12000)p;
+        return (PFN_cuTensorMapEncodeTiled_v12000)nullptr;
+    }();
     return fn;
 }
 
@@ -891,7 +891,7 @@ struct Plan {
 // separate streams); slot 0 serves every single-matrix entry point.
 constexpr int kPlanSlots = 8;
 Plan g_plans[kPlanSlots];
-int g_plan_slot = 0;
+thread_local int g_plan_slot = 0;
 inline Plan& cur_plan() { return g_plans[g_plan_slot]; }
 
 struct Carve {
@@ -1020,18 +1020,16 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     if (!rc) rc = make_map3(&P.map_bdig16, P.bdig, P.kpad, 16, KD_MAX, P.kpad, 16 * P.kpad, 16);
     if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
     if (rc) return rc;
-    static bool attrs = false;
-    if (!attrs) {
-        rc = set_smem(gram_tc_kernel<6>, SmemLayout<32, 6>::BYTES);
-        if (!rc) rc = set_smem(gram_tc_kernel<7>, SmemLayout<32, 7>::BYTES);
-        if (!rc) rc = set_smem(update_tc_kernel<16, 6>, SmemLayout<16, 6>::BYTES);
-        if (!rc) rc = set_smem(update_tc_kernel<16, 7>, SmemLayout<16, 7>::BYTES);
-        if (!rc) rc = set_smem(update_tc_kernel<32, 6>, SmemLayout<32, 6>::BYTES);
-        if (!rc) rc = set_smem(update_tc_kernel<32, 7>, SmemLayout<32, 7>::BYTES);
-        if (rc) return rc;
-        attrs = true;
-    }
-    return 0;
+    static const int attrs_rc = [] {   // once, thread-safe
+        int r = set_smem(gram_tc_kernel<6>, SmemLayout<32, 6>::BYTES);
+        if (!r) r = set_smem(gram_tc_kernel<7>, SmemLayout<32, 7>::BYTES);
+        if (!r) r = set_smem(update_tc_kernel<16, 6>, SmemLayout<16, 6>::BYTES);
+        if (!r) r = set_smem(update_tc_kernel<16, 7>, SmemLayout<16, 7>::BYTES);
+        if (!r) r = set_smem(update_tc_kernel<32, 6>, SmemLayout<32, 6>::BYTES);
+        if (!r) r = set_smem(update_tc_kernel<32, 7>, SmemLayout<32, 7>::BYTES);
+        return r;
+    }();
+    return attrs_rc;
 }
 
 void split_mark_stale(int c0, int nc) {
@@ -1212,13 +1210,9 @@ int launch_fused_update_split(double* X, i64 ld, i64 m, int K, int s, int nz, co
     if (rc) return rc;
     cudaError_t ce = cudaMemsetAsync(P.bmax, 0, 128 * sizeof(unsigned long long), st);
     if (ce != cudaSuccess) return (int)ce;
-    static bool fattr = false;
-    if (!fattr) {
-        ce = cudaFuncSetAttribute(bbuild_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(3 * 64 * 65 * sizeof(double)));
-        if (ce != cudaSuccess) return (int)ce;
-        fattr = true;
-    }
+    static const cudaError_t fattr_rc = cudaFuncSetAttribute(   // once, thread-safe
+        bbuild_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(3 * 64 * 65 * sizeof(double)));
+    if (fattr_rc != cudaSuccess) return (int)fattr_rc;
     bbuild_fused_kernel<<<(unsigned)ceil_div(kin, 64), 256, 3 * 64 * 65 * sizeof(double), st>>>(G, ldg, K, s, Ty, s, Sp, ldsp, Ts, nz, nz,
                                                                         P.cexp, P.bfull, (int)P.kpad, P.bmax);
     g_launch_count += 1;

@@ -253,12 +253,9 @@ static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR
                     cudaStream_t st) {
     const int TR = tsqr_tile_rows(nc);
     const size_t smem = tsqr_tile_smem_bytes(TR, NC);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(tsqr_tile_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-        attr_set = true;
-    }
+    static const cudaError_t attr_rc = cudaFuncSetAttribute(   // once, thread-safe
+        tsqr_tile_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (attr_rc != cudaSuccess) return (int)attr_rc;
     // Level matrices: level 0 is the panel itself; level l >= 1 lives in ws.
     constexpr int kMaxLevels = 48;   // nc > 32 reduces 128 rows to 64 per level: 2^k rows need about k levels
     double* lvl_ptr[kMaxLevels];
