@@ -25,11 +25,13 @@
 // with the column scales 2^{e_c} folded into the rows of the small right-hand
 // factor, so the triangular scaling also runs on the tensor cores.
 //
-// Kernels are persistent and warp-specialized (warp 0: TMA producer, warp 1: MMA
-// issuer + TMEM owner, warps 2-5: epilogue), with an A-tile ring of 16 KB slots, a
-// B ring, and two TMEM accumulators so the epilogue of one window overlaps the MMAs
-// of the next. Every wait is bounded; a timeout sets an error word and the kernel
-// winds down.
+// Kernels are warp-specialized (warp 0: TMA producer, warp 1: MMA issuer + TMEM
+// owner, warps 2-9: epilogue, two threads per TMEM lane), with an A-tile ring of
+// 16 KB slots, a B ring, and two TMEM accumulators so the epilogue of one window
+// overlaps the MMAs of the next. The update is persistent and takes row tiles from
+// a per-launch counter; the Gram's M-block CTAs of one row range form a cluster that
+// shares each B tile by TMA multicast. Every wait is bounded; a timeout sets an
+// error word and the kernel winds down.
 #include <cstdio>
 #include <cstring>
 #include <vector>
