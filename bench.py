@@ -20,6 +20,12 @@ of the reference) on a bounded sample of the same workload on the host cores.
 
 `--impl reference` times the reference's CPU algorithm (the oracle restatement;
 the reference's own build cannot run on this host) on the host cores.
+
+Other workloads (not the default line):
+  --workload batched [--precision split]   4096 independent matrices of uneven m, s,
+      p and kappa in one batched plan (matrices/s, worst-case LOO over the batch);
+  --workload sweep [--variant V --kappas ... --block s --monomial]   accuracy and
+      time per condition number in FP64 and both split forms.
 """
 from __future__ import annotations
 
