@@ -37,6 +37,10 @@ import sys
 import threading
 import time
 
+# Split-precision batches run up to 16 concurrent streams; give each its own
+# hardware work queue (must be set before CUDA starts).
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "one-synchronization-bcgs_gb300"))
 
@@ -454,7 +458,7 @@ def run_batched(args, rank, world, local_rank):
     # Two copies of the batch (a resident pristine copy and the working one), the
     # R factors and the plan's workspace must fit.
     count = len(ms)
-    while count > 1 and 2 * 8 * sum(sizes[:count]) + 8 * sum(n * n for n in ns[:count]) + (8 << 30) > free:
+    while count > 1 and 2 * 8 * sum(sizes[:count]) + 8 * sum(n * n for n in ns[:count]) + (32 << 30) > free:
         count = int(count * 0.9)
     ms, ns, ss, ks, sizes = ms[:count], ns[:count], ss[:count], ks[:count], sizes[:count]
     offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
@@ -550,7 +554,7 @@ def run_batched(args, rank, world, local_rank):
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": None,
                 "note": "whole batch: algorithmic FP64 bytes 8m[sP(P-1)/2 + 4n] per matrix / run time; "
-                        "matrices run through the single-matrix tensor-core driver on 8 concurrent streams",
+                        "matrices run through the single-matrix tensor-core driver on up to 16 concurrent streams",
                 "tflops_fp64_equivalent": round(flops / (ms_run * 1e-3) / 1e12, 3)}
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -576,7 +580,7 @@ def run_batched(args, rank, world, local_rank):
         "config": {"workload": (f"batched bcgsi2P1s, {count} matrices (seed {args.batch_seed}), FP64, "
                                 f"one CUDA graph of {info['launches']} launches per step") if bprec == orth.FP64 else
                                (f"batched bcgsi2P1s, {count} matrices (seed {args.batch_seed}), split_bf16x7, "
-                                f"per-matrix tensor-core QRs on 8 concurrent streams ({info['launches']} launches "
+                                f"per-matrix tensor-core QRs on up to 16 concurrent streams ({info['launches']} launches "
                                 f"per step)"),
                    "batch": count, "batch_requested": args.batch, "elements": int(offs[-1]),
                    "tuned_panel_rows": {str(k): v for k, v in info["tuned"].items()},

@@ -129,8 +129,9 @@ void orth_gb300_set_gram_chunk_rows(long long rows);
  * rows per block size on the batch itself (reads X, writes only the plan's
  * scratch).
  * precision ORTH_GB300_SPLIT_BF16 / _FAST: any variant, s[b] <= 64. Each run
- * spreads the matrices over up to 8 scratch slots (longest first to the least
- * loaded slot), each on its own stream forked from and joined back into `stream`,
+ * spreads the matrices over up to 16 scratch slots (as many as fit in half of the
+ * free device memory; longest first to the least loaded slot), each on its own
+ * stream forked from and joined back into `stream`,
  * and runs them through the single-matrix tensor-core driver (no graph; a slot's
  * digit stores, 28 bytes per element, are sized for its largest matrix and
  * reused). Breakdowns and split-kernel timeouts are collected per matrix on the

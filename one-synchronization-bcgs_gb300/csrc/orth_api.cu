@@ -56,7 +56,7 @@ struct DevBuf {
 // MPI_COMM_WORLD collectives); calls are serialized by a mutex here.
 // Per-call scratch of the drivers. Slot 0 serves every entry point; split-precision
 // batches use up to kSlots slots, one per concurrent stream.
-constexpr int kSlots = 8;
+constexpr int kSlots = 16;
 struct Scratch {
     DevBuf part, small, status, tsqr, split;
 };
@@ -788,6 +788,28 @@ int split_batch_enqueue(int variant, int count, const int* m, const int* n, cons
     if (init_ctx()) return 3;
     int S = count < kSlots ? count : kSlots;
     if (max_slots >= 1 && S > max_slots) S = max_slots;
+    {
+        // Each slot's scratch is sized for its largest matrix, and the longest-first
+        // assignment gives each slot one of the S largest. Take the most slots whose
+        // S largest workspaces fit in half of the free device memory (at least one).
+        std::vector<double> wsz(count);
+        for (int b = 0; b < count; ++b)
+            wsz[b] = (double)split_workspace_bytes(m[b], n[b], s[b], g_ctx.num_sms) +
+                     8.0 * ((double)part_doubles(m[b], n[b], s[b], g_ctx.num_sms) +
+                            (double)tsqr_workspace_doubles(m[b], s[b]));
+        std::sort(wsz.begin(), wsz.end(), [](double a, double b) { return a > b; });
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+            double acc = 0.0;
+            int fit = 0;
+            for (int k = 0; k < S; ++k) {
+                acc += wsz[k];
+                if (acc > 0.5 * (double)free_b) break;
+                fit = k + 1;
+            }
+            S = fit > 1 ? fit : 1;
+        }
+    }
     // Longest job (m n^2) first, each to the least loaded slot.
     std::vector<int> order(count), slot_of(count);
     for (int b = 0; b < count; ++b) order[b] = b;

@@ -891,7 +891,7 @@ struct Plan {
 };
 // One plan per scratch slot (split-precision batches run several at once on
 // separate streams); slot 0 serves every single-matrix entry point.
-constexpr int kPlanSlots = 8;
+constexpr int kPlanSlots = 16;
 Plan g_plans[kPlanSlots];
 thread_local int g_plan_slot = 0;
 inline Plan& cur_plan() { return g_plans[g_plan_slot]; }
