@@ -334,7 +334,7 @@ def run_ours(args, rank, world, local_rank):
         Rh = Rh_t.numpy().T
         work = np.zeros(1)
         orth.set_host_precision(prec)
-        times = []
+        times, timelines = [], []
         for k in range(args.e2e_steps + 1):
             Xh_t.copy_(X0, non_blocking=False)
             Rh_t.zero_()
@@ -346,8 +346,11 @@ def run_ours(args, rank, world, local_rank):
                 raise RuntimeError(f"host entry point rc={rc}")
             if k > 0:   # first call warms the host-path buffers
                 times.append(dt * 1e3)
+                timelines.append(orth.last_host_timing())
         e2e_ms = max_over_ranks(sum(times) / len(times), world, dev)
         e2e = {"value": round(e2e_ms, 3), "unit": "ms", "samples_ms": [round(x, 1) for x in times],
+               "timeline_ms": {key: round(sum(t[key] for t in timelines) / len(timelines), 1)
+                               for key in timelines[0]},
                "h2d_bytes_per_step": m * n * 8, "d2h_bytes_per_step": m * n * 8 + n * n * 8,
                "path": f"orth.h {variant} (host pointers, pinned), {prec_name}"}
         del Xh_t, Rh_t

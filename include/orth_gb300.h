@@ -172,6 +172,14 @@ int orth_gb300_poison_shared_memory(unsigned long long bits, void *stream);
 /* Status of the last run through the orth.h entry points on this thread. */
 void orth_gb300_last_status(orth_gb300_status *status);
 
+/*
+ * Timeline of the last successful orth.h host-buffer run on this thread, in ms:
+ * out[0] all of X on the device, out[1] compute stream done (R staged), out[2]
+ * last Q chunk back on the host, each from the run's first device operation;
+ * out[3] the call's wall time. Zeros before the first such run.
+ */
+void orth_gb300_last_host_timing(double out[4]);
+
 /* Number of device-wide reductions ("synchronizations") a call performs. */
 int orth_gb300_sync_count(int variant, int n, int s);
 

@@ -58,6 +58,8 @@ def load(path: str | None = None):
     lib.orth_gb300_run_dev.restype = ctypes.c_int
     lib.orth_gb300_last_status.argtypes = [ctypes.POINTER(Status)]
     lib.orth_gb300_last_status.restype = None
+    lib.orth_gb300_last_host_timing.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    lib.orth_gb300_last_host_timing.restype = None
     lib.orth_gb300_sync_count.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.orth_gb300_sync_count.restype = ctypes.c_int
     lib.orth_gb300_last_launch_count.argtypes = []
@@ -157,6 +159,14 @@ def last_status() -> dict:
     st = Status()
     load().orth_gb300_last_status(ctypes.byref(st))
     return st.as_dict()
+
+
+def last_host_timing() -> dict:
+    """Timeline of this thread's last orth.h host-buffer run, in ms from its first
+    device operation: X resident, compute done, Q back; and the call's wall time."""
+    out = (ctypes.c_double * 4)()
+    load().orth_gb300_last_host_timing(out)
+    return {"x_resident_ms": out[0], "compute_done_ms": out[1], "q_back_ms": out[2], "wall_ms": out[3]}
 
 
 def run_dev(variant: str, m: int, n: int, s: int, x_ptr: int, ldx: int, r_ptr: int, ldr: int,

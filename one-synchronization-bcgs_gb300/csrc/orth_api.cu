@@ -6,6 +6,7 @@
 // deterministic device-wide reduction and every small s x s step kept on the
 // device, so a whole QR is enqueued on one stream with no host round trip.
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cstdio>
 #include <cstdlib>
@@ -71,6 +72,9 @@ struct Context {
     size_t hostR_stage_bytes = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_in = nullptr, copy_out = nullptr;   // host-path column transfers
+    // Host-path timeline: call start, last H2D chunk landed, compute stream done
+    // (R staged), last D2H chunk landed.
+    cudaEvent_t host_ev[4] = {};
     int num_sms = kNumSMsDefault;
     bool init = false;
 };
@@ -124,6 +128,9 @@ struct ProfScope {
     }
 };
 thread_local orth_gb300_status g_last_status = {0, 0, 0, 0};
+// Timeline of this thread's last host-buffer run (ms from its first device
+// operation): X resident, compute done, Q and R back; then the call's wall time.
+thread_local double g_last_host_timing[4] = {0, 0, 0, 0};
 
 // Precision of the orth.h host entry points: FP64 (the reference's arithmetic)
 // unless set through orth_gb300_set_host_precision or ORTH_GB300_PRECISION
@@ -148,6 +155,7 @@ int init_ctx() {
     BCGS_CUDA_TRY(cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking));
     BCGS_CUDA_TRY(cudaStreamCreateWithFlags(&g_ctx.copy_in, cudaStreamNonBlocking));
     BCGS_CUDA_TRY(cudaStreamCreateWithFlags(&g_ctx.copy_out, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : g_ctx.host_ev) BCGS_CUDA_TRY(cudaEventCreate(&e));
     g_ctx.init = true;
     return 0;
 }
@@ -731,10 +739,15 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
         const i64 per64mb = ((i64)64 << 20) / ((i64)m * (i64)sizeof(double));
         link.chunk = (int)(per64mb > s ? (per64mb < n ? per64mb : n) : s);
     }
-    cudaError_t ce = cudaMemsetAsync(dR, 0, rbytes, st);
+    const auto wall0 = std::chrono::steady_clock::now();
+    cudaEvent_t* tev = g_ctx.host_ev;
+    bool timed = false;
+    cudaError_t ce = cudaEventRecord(tev[0], st);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(dR, 0, rbytes, st);
     if (ce == cudaSuccess) {
         link.start(st);
         ce = (cudaError_t)link.err;
+        if (ce == cudaSuccess) ce = cudaEventRecord(tev[1], g_ctx.copy_in);
     }
     if (ce == cudaSuccess) {
         rc = run_device(variant, m, n, s, dX, m, dR, n, precision, st, &stt, &link);
@@ -742,6 +755,9 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
             link.final(st, n);
             ce = (cudaError_t)link.err;
             if (ce == cudaSuccess) ce = cudaMemcpyAsync(g_ctx.hostR_stage, dR, rbytes, cudaMemcpyDeviceToHost, st);
+            if (ce == cudaSuccess) ce = cudaEventRecord(tev[2], st);
+            if (ce == cudaSuccess) ce = cudaEventRecord(tev[3], g_ctx.copy_out);
+            timed = ce == cudaSuccess;
         }
     }
     // The caller's buffer is in use until both copy streams are done, on every path.
@@ -749,6 +765,14 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
     cudaError_t c2 = cudaStreamSynchronize(g_ctx.copy_out);
     cudaError_t c3 = cudaStreamSynchronize(st);
     link.release();
+    if (timed && c1 == cudaSuccess && c2 == cudaSuccess && c3 == cudaSuccess) {
+        for (int k = 1; k < 4; ++k) {
+            float ms = 0.f;
+            g_last_host_timing[k - 1] = cudaEventElapsedTime(&ms, tev[0], tev[k]) == cudaSuccess ? ms : -1.0;
+        }
+        g_last_host_timing[3] =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
+    }
     if (ce == cudaSuccess) ce = c1 != cudaSuccess ? c1 : (c2 != cudaSuccess ? c2 : c3);
     if (rc) {
         g_last_status = stt;
@@ -904,6 +928,11 @@ int orth_gb300_run_dev(int variant, int m, int n, int s, double* dX, long long l
 
 void orth_gb300_last_status(orth_gb300_status* status) {
     if (status) *status = g_last_status;
+}
+
+void orth_gb300_last_host_timing(double out[4]) {
+    if (out)
+        for (int k = 0; k < 4; ++k) out[k] = g_last_host_timing[k];
 }
 
 int orth_gb300_set_host_precision(int precision) {
