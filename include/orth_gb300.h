@@ -69,7 +69,7 @@ int orth_gb300_bcgsi2P1s_dev_noalloc(int m, int n, int s, double *dX, long long 
  * Precision used by the five orth.h entry points (default ORTH_GB300_FP64, the
  * reference's arithmetic; the environment variable ORTH_GB300_PRECISION =
  * fp64 | split | split_fast sets it at first use). Shapes the split modes do not
- * handle (s > 32) return 4. Returns 0, or 4 for an unknown mode.
+ * handle (s > 64) return 4. Returns 0, or 4 for an unknown mode.
  */
 int orth_gb300_set_host_precision(int precision);
 
@@ -174,9 +174,9 @@ void orth_gb300_last_status(orth_gb300_status *status);
 
 /*
  * Timeline of the last successful orth.h host-buffer run on this thread, in ms:
- * out[0] all of X on the device, out[1] compute stream done (R staged), out[2]
- * last Q chunk back on the host, each from the run's first device operation;
- * out[3] the call's wall time. Zeros before the first such run.
+ * out[0] all of X on the device, out[1] the QR's kernels done, out[2] last Q
+ * chunk back on the host, each from the run's first device operation; out[3] the
+ * call's wall time. Zeros before the first such run.
  */
 void orth_gb300_last_host_timing(double out[4]);
 

@@ -471,7 +471,7 @@ void build_schedule(BatchPlan& P, Blob& blob) {
 int enqueue_all(BatchPlan& P, cudaStream_t st) {
     const char* base = (const char*)P.jobs_dev;
     long long l0 = g_launch_count;
-    cudaError_t ce = cudaMemsetAsync(P.mats[0].status, 0, (size_t)P.count * kStatusWords * sizeof(int), st);
+    cudaError_t ce = (cudaError_t)zero_async(P.mats[0].status, (size_t)P.count * kStatusWords * sizeof(int), st);
     if (ce != cudaSuccess) return (int)ce;
     for (const Stage& S : P.stages) {
         const int* prefix = (const int*)(base + S.prefix_off);

@@ -15,6 +15,9 @@ using i64 = long long;
 // split-precision batches enqueue from several host threads).
 extern std::atomic<long long> g_launch_count;
 
+// bytes of zeros at p, by a kernel on st (not a copy-engine memset).
+int zero_async(void* p, size_t bytes, cudaStream_t st);
+
 // C (na x nb, ld ldo) = X[:, a0:a0+na]^T X[:, b0:b0+nb] over m rows, FP64, with a
 // fixed-order two-stage reduction through `part` (nchunks * na * nb doubles).
 int gram_chunks_fp64(i64 m, int na, int nb, int num_sms);

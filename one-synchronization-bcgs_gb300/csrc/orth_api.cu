@@ -72,8 +72,8 @@ struct Context {
     size_t hostR_stage_bytes = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_in = nullptr, copy_out = nullptr;   // host-path column transfers
-    // Host-path timeline: call start, last H2D chunk landed, compute stream done
-    // (R staged), last D2H chunk landed.
+    // Host-path timeline: call start, last H2D chunk landed, the QR's kernels done,
+    // last D2H chunk landed.
     cudaEvent_t host_ev[4] = {};
     int num_sms = kNumSMsDefault;
     bool init = false;
@@ -218,7 +218,8 @@ int reserve(i64 m, int n, int s, int precision) {
 
 // ---------------------------------------------------------------------------
 // Host-buffer runs (the orth.h entry points): X arrives in column chunks on one
-// copy stream and Q leaves on another while the QR runs. The compute stream waits
+// copy stream and Q leaves on another while the QR runs; the two directions
+// overlap on the link. The compute stream waits
 // only for the chunks a primitive reads (need). Every update or TSQR that writes
 // from column c0 marks columns [0, c0) final (final). No variant writes a column
 // left of the block it is working on, so those columns can be copied back at once.
@@ -272,6 +273,21 @@ struct HostLink {
         if (!err) err = (int)cudaStreamWaitEvent(cout, ev_fin, 0);
         if (!err) err = (int)copy(hX, ldh, dX, m, out_done, c_end - out_done, cudaMemcpyDeviceToHost, cout);
         out_done = c_end;
+    }
+    // The last columns of Q and all of R, enqueued before the caller reads the run's
+    // status, so that they do not wait for that read. R goes to the staging buffer
+    // hR on the compute stream; done (if set) is recorded there when the QR's
+    // kernels have finished, before R's copy.
+    double* hR = nullptr;
+    const double* dR = nullptr;
+    size_t rbytes = 0;
+    cudaEvent_t done = nullptr;
+    bool finished = false;
+    void finish(cudaStream_t st) {
+        final(st, n);
+        if (!err && done) err = (int)cudaEventRecord(done, st);
+        if (!err) err = (int)cudaMemcpyAsync(hR, dR, rbytes, cudaMemcpyDeviceToHost, st);
+        finished = !err;
     }
     void release() {
         for (cudaEvent_t e : ev_in) cudaEventDestroy(e);
@@ -659,7 +675,7 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
     Engine e{dX, (i64)ldX, (i64)m, n, s, dR, ldR, precision, st,
              carve_small(scr().small.as<double>(), n, s), scr().status.as<int>()};
     e.link = link;
-    cudaError_t ce = cudaMemsetAsync(e.status, 0, kStatusWords * sizeof(int), st);
+    cudaError_t ce = (cudaError_t)zero_async(e.status, kStatusWords * sizeof(int), st);
     if (ce != cudaSuccess) e.err = (int)ce;
     if (!e.err && is_split(precision))
         e.err = split_begin(dX, ldX, m, n, s, split_digits_of(precision), scr().split.as<char>(), scr().split.bytes, g_ctx.num_sms, st);
@@ -675,6 +691,10 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
         default: run_p2s(e); break;
     }
     g_last_launches = g_launch_count - launches0;
+    if (link && !e.err) {
+        link->finish(st);
+        if (link->err) e.err = link->err;
+    }
     if (out) {
         std::memset(out, 0, sizeof(*out));
         int h[kStatusWords] = {0, 0, 0, 0};
@@ -735,6 +755,7 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
     HostLink link;
     link.hX = Xsub; link.ldh = ldXsub; link.m = m; link.n = n; link.dX = dX;
     link.cin = g_ctx.copy_in; link.cout = g_ctx.copy_out;
+    link.hR = g_ctx.hostR_stage; link.dR = dR; link.rbytes = rbytes;
     {
         const i64 per64mb = ((i64)64 << 20) / ((i64)m * (i64)sizeof(double));
         link.chunk = (int)(per64mb > s ? (per64mb < n ? per64mb : n) : s);
@@ -743,19 +764,17 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
     cudaEvent_t* tev = g_ctx.host_ev;
     bool timed = false;
     cudaError_t ce = cudaEventRecord(tev[0], st);
-    if (ce == cudaSuccess) ce = cudaMemsetAsync(dR, 0, rbytes, st);
+    if (ce == cudaSuccess) ce = (cudaError_t)zero_async(dR, rbytes, st);
     if (ce == cudaSuccess) {
         link.start(st);
         ce = (cudaError_t)link.err;
         if (ce == cudaSuccess) ce = cudaEventRecord(tev[1], g_ctx.copy_in);
     }
+    link.done = tev[2];
     if (ce == cudaSuccess) {
         rc = run_device(variant, m, n, s, dX, m, dR, n, precision, st, &stt, &link);
         if (!rc) {
-            link.final(st, n);
-            ce = (cudaError_t)link.err;
-            if (ce == cudaSuccess) ce = cudaMemcpyAsync(g_ctx.hostR_stage, dR, rbytes, cudaMemcpyDeviceToHost, st);
-            if (ce == cudaSuccess) ce = cudaEventRecord(tev[2], st);
+            ce = link.finished ? (cudaError_t)link.err : cudaErrorUnknown;
             if (ce == cudaSuccess) ce = cudaEventRecord(tev[3], g_ctx.copy_out);
             timed = ce == cudaSuccess;
         }

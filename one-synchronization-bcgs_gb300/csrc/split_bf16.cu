@@ -955,7 +955,7 @@ int ensure_fresh(int c_begin, int c_end, cudaStream_t st) {
         while (e < c_end && !P.fresh[e] && e - c < 32 && P.cmax_valid[e] == P.cmax_valid[c]) ++e;
         const int nc = e - c;
         if (!P.cmax_valid[c]) {
-            cudaError_t ce = cudaMemsetAsync(P.cmax + c, 0, (size_t)nc * sizeof(unsigned long long), st);
+            cudaError_t ce = (cudaError_t)zero_async(P.cmax + c, (size_t)nc * sizeof(unsigned long long), st);
             if (ce != cudaSuccess) return (int)ce;
             dim3 g1((unsigned)ceil_div(P.m, 4096), (unsigned)nc);
             colmax_kernel<<<g1, 256, 0, st>>>(P.X, P.ld, P.m, c, P.cmax);
@@ -1006,14 +1006,14 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     // the last K chunk of an update reads columns past K + nc, multiplied by zero
     // rows of the factor. Repeated runs of one shape keep their zeroed padding.
     if (P.zeroed_base != (const void*)P.colstore || P.zeroed_m != m || P.zeroed_n != n) {
-        cudaError_t ce = cudaMemsetAsync(P.colstore, 0, (size_t)KD_MAX * P.nrc * 64 * n * 2, st);
-        if (ce == cudaSuccess) ce = cudaMemsetAsync(P.rowstore, 0, (size_t)KD_MAX * P.ncc * 64 * m * 2, st);
+        cudaError_t ce = (cudaError_t)zero_async(P.colstore, (size_t)KD_MAX * P.nrc * 64 * n * 2, st);
+        if (ce == cudaSuccess) ce = (cudaError_t)zero_async(P.rowstore, (size_t)KD_MAX * P.ncc * 64 * m * 2, st);
         if (ce != cudaSuccess) return (int)ce;
         P.zeroed_base = P.colstore;
         P.zeroed_m = m;
         P.zeroed_n = n;
     }
-    cudaError_t ce = cudaMemsetAsync(P.err, 0, sizeof(int), st);
+    cudaError_t ce = (cudaError_t)zero_async(P.err, sizeof(int), st);
     if (ce != cudaSuccess) return (int)ce;
     // Chunked stores as 3-D tensors {64, columns or rows, plane x chunk}.
     int rc = make_map3(&P.map_col_a, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, TILE_M);
@@ -1161,13 +1161,13 @@ static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int 
             bdigit_kernel<7><<<(unsigned)ceil_div(P.kpad, 256), 256, 0, st>>>(Bg, (int)P.kpad, kin - ng, ng, NB,
                                                                                (int)P.kpad, P.bmax + j0, P.fexp,
                                                                                P.bdig);
-        cudaError_t ce = cudaMemsetAsync(P.cmax + c0 + j0, 0, (size_t)ng * sizeof(unsigned long long), st);
+        cudaError_t ce = (cudaError_t)zero_async(P.cmax + c0 + j0, (size_t)ng * sizeof(unsigned long long), st);
         if (ce != cudaSuccess) return (int)ce;
         UpdateParams up;
         up.ncc = (int)P.ncc;
         up.m = m; up.kin = kin; up.nc = ng; up.c0 = c0 + j0; up.ld = ld; up.X = X; up.fexp = P.fexp;
         up.cmax = P.cmax; up.err = P.err; up.tile_ctr = P.tile_ctr;
-        ce = cudaMemsetAsync(P.tile_ctr, 0, sizeof(int), st);
+        ce = (cudaError_t)zero_async(P.tile_ctr, sizeof(int), st);
         if (ce != cudaSuccess) return (int)ce;
         const int ntiles = (int)ceil_div(m, TILE_M);
         const int grid = ntiles < num_sms ? ntiles : num_sms;
@@ -1193,7 +1193,7 @@ int launch_update_split(double* X, i64 ld, i64 m, int K, int c0, int nc, const d
     if (c0 != K || nc > 64 || X != P.X) return (int)cudaErrorInvalidValue;
     int rc = ensure_fresh(0, K + nc, st);
     if (rc) return rc;
-    cudaError_t ce = cudaMemsetAsync(P.bmax, 0, 64 * sizeof(unsigned long long), st);
+    cudaError_t ce = (cudaError_t)zero_async(P.bmax, 64 * sizeof(unsigned long long), st);
     if (ce != cudaSuccess) return (int)ce;
     const int kin = K + nc;
     bbuild_kernel<<<(unsigned)ceil_div(kin, 64), 256, 0, st>>>(S, lds, T, ldt, K, nc, P.cexp, P.bfull,
@@ -1210,7 +1210,7 @@ int launch_fused_update_split(double* X, i64 ld, i64 m, int K, int s, int nz, co
     if (s > 64 || nz > 64 || X != P.X) return (int)cudaErrorInvalidValue;
     int rc = ensure_fresh(0, kin, st);
     if (rc) return rc;
-    cudaError_t ce = cudaMemsetAsync(P.bmax, 0, 128 * sizeof(unsigned long long), st);
+    cudaError_t ce = (cudaError_t)zero_async(P.bmax, 128 * sizeof(unsigned long long), st);
     if (ce != cudaSuccess) return (int)ce;
     static const cudaError_t fattr_rc = cudaFuncSetAttribute(   // once, thread-safe
         bbuild_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(3 * 64 * 65 * sizeof(double)));
