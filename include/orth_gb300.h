@@ -133,7 +133,7 @@ void orth_gb300_set_gram_chunk_rows(long long rows);
  * free device memory; longest first to the least loaded slot), each on its own
  * stream forked from and joined back into `stream`,
  * and runs them through the single-matrix tensor-core driver (no graph; a slot's
- * digit stores, 28 bytes per element, are sized for its largest matrix and
+ * digit store, 14 bytes per element, is sized for its largest matrix and
  * reused). Breakdowns and split-kernel timeouts are collected per matrix on the
  * device. The slots are the library's own scratch: order any later library call
  * after the run (same stream, or a synchronize).

@@ -12,6 +12,8 @@
 
 namespace bcgs {
 
+std::atomic<long long> g_aux_launch_count{0};
+
 namespace {
 
 // Bytes [0, head) and [head + 16 n16, head + 16 n16 + tail) one at a time; the
@@ -41,6 +43,7 @@ int zero_async(void* p, size_t bytes, cudaStream_t st) {
     const unsigned grid = (unsigned)(want < 1 ? 1 : (want > cap ? cap : want));
     zero_kernel<<<grid, 256, 0, st>>>(b, (int)head, n16, tail);
     ++g_launch_count;
+    ++g_aux_launch_count;
     return (int)cudaGetLastError();
 }
 

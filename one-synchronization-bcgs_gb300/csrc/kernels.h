@@ -15,8 +15,11 @@ using i64 = long long;
 // split-precision batches enqueue from several host threads).
 extern std::atomic<long long> g_launch_count;
 
-// bytes of zeros at p, by a kernel on st (not a copy-engine memset).
+// bytes of zeros at p, by a kernel on st (not a copy-engine memset). Counted in
+// g_launch_count and also in g_aux_launch_count, which the per-class profile
+// subtracts so that its launch counts are those of the classes' own kernels.
 int zero_async(void* p, size_t bytes, cudaStream_t st);
+extern std::atomic<long long> g_aux_launch_count;
 
 // C (na x nb, ld ldo) = X[:, a0:a0+na]^T X[:, b0:b0+nb] over m rows, FP64, with a
 // fixed-order two-stage reduction through `part` (nchunks * na * nb doubles).

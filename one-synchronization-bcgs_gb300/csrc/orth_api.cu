@@ -112,7 +112,8 @@ struct ProfScope {
     cudaStream_t st;
     cudaEvent_t a = nullptr;
     long long l0;
-    ProfScope(int c, cudaStream_t s, double flops, double bytes) : cls(c), st(s), l0(g_launch_count) {
+    ProfScope(int c, cudaStream_t s, double flops, double bytes)
+        : cls(c), st(s), l0(g_launch_count - g_aux_launch_count) {
         if (!g_prof.on) return;
         a = g_prof.get();
         cudaEventRecord(a, st);
@@ -124,7 +125,7 @@ struct ProfScope {
         cudaEvent_t b = g_prof.get();
         cudaEventRecord(b, st);
         g_prof.pending.push_back({cls, a, b});
-        g_prof.launches[cls] += g_launch_count - l0;
+        g_prof.launches[cls] += g_launch_count - g_aux_launch_count - l0;
     }
 };
 thread_local orth_gb300_status g_last_status = {0, 0, 0, 0};
@@ -819,7 +820,7 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
 }  // namespace
 
 // Split-precision batches: the matrices one after another on `st` through the
-// single-matrix driver (its digit stores are 28 bytes per element, so a whole
+// single-matrix driver (its digit store is 14 bytes per element, so a whole
 // batch's stores at once would not fit). Workspaces are grown for the largest
 // shapes first, so no allocation happens between matrices. After each matrix its
 // status words (4 ints) and the split kernels' error word go to dstatus[8 b ..]

@@ -14,12 +14,15 @@
 // accumulator every 256 summation steps into two 64-bit integers; group g = 8
 // (weight 2^-48 relative) is summed in FP32.
 //
-// Two digit stores serve the two product shapes, both K-major for the tensor core
-// and chunked so that every 128 x 64 TMA tile is one contiguous 16 KB block of HBM:
-//   column store [plane][64-row chunk][column][64 rows]: A and B of the tall Gram
-//                X[:, 0:na]^T X[:, b0:b0+nb] (sum over rows)
-//   row store    [plane][64-column chunk][row][64 columns]: A of the update
-//                [Q | X_k] * B (sum over columns)
+// One digit store serves both product shapes. It is chunked so that every TMA
+// tile is one contiguous block of HBM:
+//   column store [plane][64-row chunk][column][64 rows]
+// The tall Gram X[:, 0:na]^T X[:, b0:b0+nb] (sum over rows) reads its A and B
+// tiles K-major: 64 rows of one column are one 128-byte swizzle row. The update
+// [Q | X_k] * B (sum over columns) reads its A tile, 128 rows x 64 columns, from
+// two adjacent 64-row chunks of the same store as an MN-major operand: there the
+// 128-byte rows run along M. Slicing a column writes 2 bytes per digit per
+// element once.
 // The update (X_k - Q S) T^{-1} is evaluated as one product
 //     [Q | X_k] * [-S T^{-1} ; T^{-1}]
 // with the column scales 2^{e_c} folded into the rows of the small right-hand
@@ -134,19 +137,17 @@ __global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c
     }
 }
 
-// Slice columns [c0, c0+nc) of X into both digit stores. A CTA handles 128 rows x
+// Slice columns [c0, c0+nc) of X into the digit store. A CTA handles 128 rows x
 // 16 columns (grid: row tiles x column groups), one row per thread: 16 coalesced
-// column loads and the digits, staged in shared memory as [plane][column][row].
-// Both stores are then written from the staging in whole 32-byte sectors:
-//   * column store: per (plane, column) two 128-byte runs (64 rows each);
-//   * row store: per (plane, row) one 32-byte sector (16 columns), written by a
-//     pair of lanes, so one warp store covers 16 complete sectors.
+// column loads and the digits, staged in shared memory as [plane][column][row],
+// then written per (plane, column) as two 128-byte runs (64 rows each) in 16-byte
+// pieces.
 template <int KD>
 __global__ void __launch_bounds__(128, 6)
 slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
              const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
-             unsigned short* __restrict__ colstore, i64 nrc, unsigned short* __restrict__ rowstore, i64 ncc) {
-    constexpr int CG = 16;                   // columns per CTA (one 32-byte row-store sector)
+             unsigned short* __restrict__ colstore, i64 nrc) {
+    constexpr int CG = 16;                   // columns per CTA
     __shared__ __align__(16) unsigned short sdig[KD][CG][128];
     const int t = threadIdx.x;
     const int g = blockIdx.y * CG;           // first column of this group (relative to c0)
@@ -165,30 +166,8 @@ slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
     }
     __syncthreads();
     const bool full = (r0 + 128 <= m);
-    // Row store: element (r, c) of plane i at ((i*ncc + c/64)*m + r)*64 + c%64.
-    const int cb = c0 + g;
-    const bool vec = (g + CG <= nc) && ((cb & 15) == 0);   // 16 columns in one 64-column chunk
-    if (vec && full) {
-        for (int e = t; e < KD * 128 * 2; e += 128) {
-            const int i = e >> 8, rr = (e & 255) >> 1, h = e & 1;
-            uint32_t w[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                w[q] = (uint32_t)sdig[i][8 * h + 2 * q][rr] | ((uint32_t)sdig[i][8 * h + 2 * q + 1][rr] << 16);
-            unsigned short* dst = rowstore + (((i64)i * ncc + cb / 64) * m + r0 + rr) * 64 + (cb & 63) + 8 * h;
-            *reinterpret_cast<uint4*>(dst) = make_uint4(w[0], w[1], w[2], w[3]);
-        }
-    } else if (r < m) {
-#pragma unroll
-        for (int i = 0; i < KD; ++i)
-#pragma unroll
-            for (int j = 0; j < CG; ++j) {
-                const int c = cb + j;
-                if (g + j < nc) rowstore[(((i64)i * ncc + c / 64) * m + r) * 64 + (c & 63)] = sdig[i][j][t];
-            }
-    }
-    // Column store: element (r, c) of plane i at ((i*nrc + r/64)*n + c)*64 + r%64; per
-    // (plane, column) the CTA's 128 rows are two 128-byte runs = 16 pieces of 16 bytes.
+    // Element (r, c) of plane i at ((i*nrc + r/64)*n + c)*64 + r%64; per (plane,
+    // column) the CTA's 128 rows are two 128-byte runs = 16 pieces of 16 bytes.
     for (int e = t; e < KD * CG * 16; e += 128) {
         const int piece = e & 15, ij = e >> 4;
         const int i = ij / CG, j = ij % CG;
@@ -502,8 +481,9 @@ __device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapA, const CUt
     return true;
 }
 
-// MMA issuer for one chunk into TMEM buffer `dcol` (column offset).
-template <int NB, int KD>
+// MMA issuer for one chunk into TMEM buffer `dcol` (column offset). A_MN: the A
+// tile is two 64-row blocks (LBO 8 KB apart) of 64 K-rows of 128 bytes (MN-major).
+template <int NB, int KD, bool A_MN = false>
 __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uint8_t* sA, uint8_t* sB,
                                           Bars* bars, Ring& ra, Ring& rb, bool first_in_window,
                                           volatile int* abort, int* err, int cs = 1) {
@@ -515,10 +495,12 @@ __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uin
         if (!tc::mbar_wait(&bars->a_full[ra.slot], ra.phase, abort, err, 22 + 100 * ra.slot)) return false;
         tc::tc_fence_after();
         const uint32_t a_addr = tc::smem_u32(sA + ra.slot * A_SLOT);
-        const uint32_t idesc = tc::idesc_bf16_f32(TILE_M, NB * (KD - i));
+        const uint32_t idesc = A_MN ? tc::idesc_bf16_f32_amn(TILE_M, NB * (KD - i))
+                                    : tc::idesc_bf16_f32(TILE_M, NB * (KD - i));
 #pragma unroll
         for (int k = 0; k < KCH / 16; ++k) {
-            const uint64_t da = tc::sw128_desc(a_addr + k * 32);
+            const uint64_t da = A_MN ? tc::sw128_desc_mn(a_addr + k * 16 * 128, 64 * KCH * 2)
+                                     : tc::sw128_desc(a_addr + k * 32);
             const uint64_t db = tc::sw128_desc(b_addr + k * 32);
             const uint32_t acc = (first_in_window && i == 0 && k == 0) ? 0u : 1u;
             tc::mma_bf16(tmem_base + dcol + (uint32_t)(i * NB), da, db, idesc, acc);
@@ -687,7 +669,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
 // ---------------------------------------------------------------------------
 struct UpdateParams {
     i64 m;
-    int ncc;      // 64-column chunks of the row store
+    int nrc;      // 64-row chunks of the column store
     int kin;      // K + nc (inner length)
     int nc, c0;
     i64 ld;
@@ -719,7 +701,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     __syncthreads();
 
     auto coords = [&](int tile, int ch, int& ax, int& ay, int& az, int& azs, int& bx, int& by, int& bz, int& bzs) {
-        ax = 0; ay = tile * TILE_M; az = ch; azs = p.ncc;   // 64-column chunk of the row store
+        ax = 0; ay = ch * KCH; az = 2 * tile; azs = p.nrc;   // 64 columns x two 64-row chunks
         bx = ch * KCH; by = 0; bz = 0; bzs = 1;
     };
 
@@ -762,8 +744,8 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
                     tc::tc_fence_after();
                     const int c_end = min(nchunks, (w + 1) * WIN);
                     for (int ch = w * WIN; ch < c_end && ok; ++ch)
-                        ok = mma_chunk<NB, KD>(tmem, (uint32_t)(buf * L::TMEM_COLS_PER_BUF), sA, sB, bars, ra, rb,
-                                           ch == w * WIN, &abort_flag, p.err);
+                        ok = mma_chunk<NB, KD, true>(tmem, (uint32_t)(buf * L::TMEM_COLS_PER_BUF), sA, sB, bars, ra,
+                                                     rb, ch == w * WIN, &abort_flag, p.err);
                     if (ok) tc::mma_commit(&bars->t_full[buf]);
                 }
             }
@@ -851,14 +833,14 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// 3-D BF16 map: dims {inner, outer, planes}, strides in bytes, box {64, box_outer, 1}.
+// 3-D BF16 map: dims {inner, outer, planes}, strides in bytes, box {64, box_outer, box_planes}.
 int make_map3(CUtensorMap* map, void* base, i64 inner, i64 outer, i64 planes, i64 ld_elems,
-              i64 plane_elems, int box_outer) {
+              i64 plane_elems, int box_outer, int box_planes = 1) {
     auto enc = encode_fn();
     if (!enc) return (int)cudaErrorNotSupported;
     cuuint64_t dims[3] = {(cuuint64_t)inner, (cuuint64_t)outer, (cuuint64_t)planes};
     cuuint64_t strides[2] = {(cuuint64_t)ld_elems * 2, (cuuint64_t)plane_elems * 2};
-    cuuint32_t box[3] = {(cuuint32_t)KCH, (cuuint32_t)box_outer, 1};
+    cuuint32_t box[3] = {(cuuint32_t)KCH, (cuuint32_t)box_outer, (cuuint32_t)box_planes};
     cuuint32_t es[3] = {1, 1, 1};
     CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -873,15 +855,15 @@ struct Plan {
     double* X = nullptr;
     i64 ld = 0, m = 0;
     int n = 0, num_sms = kNumSMsDefault;
-    i64 nrc = 0, ncc = 0, kpad = 0;   // 64-row chunks (column store), 64-column chunks (row store)
+    i64 nrc = 0, kpad = 0;   // 64-row chunks of the column store; n rounded up to 64
     // device buffers (carved from the workspace)
-    unsigned short *colstore = nullptr, *rowstore = nullptr, *bdig = nullptr;
+    unsigned short *colstore = nullptr, *bdig = nullptr;
     int *cexp = nullptr, *fexp = nullptr, *err = nullptr, *tile_ctr = nullptr;
     unsigned long long *cmax = nullptr, *bmax = nullptr;
     double *bfull = nullptr, *part = nullptr;
     i64 part_doubles = 0;
     // maps
-    CUtensorMap map_col_a, map_col_b, map_row_a, map_bdig16, map_bdig32;
+    CUtensorMap map_col_a, map_col_b, map_col_u, map_bdig16, map_bdig32;
     int kd = 7;
     std::vector<char> fresh;
     std::vector<char> cmax_valid;   // cmax[c] already holds max |X[:, c]| (set by the update)
@@ -923,9 +905,8 @@ i64 gram_part_doubles(i64 m, int n, int s, int num_sms) {
 
 size_t layout_bytes(i64 m, int n, int s, int num_sms, Plan* out, char* base) {
     Carve cv{base};
-    const i64 nrc = ceil_div(m, 64), ncc = ceil_div(n, 64), kpad = round_up(n, 64);
+    const i64 nrc = ceil_div(m, 64), kpad = round_up(n, 64);
     unsigned short* col = cv.take<unsigned short>((i64)KD_MAX * nrc * n * 64);
-    unsigned short* row = cv.take<unsigned short>((i64)KD_MAX * ncc * m * 64);
     unsigned short* bd = cv.take<unsigned short>((i64)KD_MAX * 32 * kpad);
     int* cexp = cv.take<int>(n + 64);
     int* fexp = cv.take<int>(64);
@@ -937,8 +918,8 @@ size_t layout_bytes(i64 m, int n, int s, int num_sms, Plan* out, char* base) {
     const i64 pd = gram_part_doubles(m, n, s, num_sms);
     double* part = cv.take<double>(pd);
     if (out) {
-        out->nrc = nrc; out->ncc = ncc; out->kpad = kpad;
-        out->colstore = col; out->rowstore = row; out->bdig = bd;
+        out->nrc = nrc; out->kpad = kpad;
+        out->colstore = col; out->bdig = bd;
         out->cexp = cexp; out->fexp = fexp; out->err = err; out->tile_ctr = tctr;
         out->cmax = cmax; out->bmax = bmax; out->bfull = bfull; out->part = part;
         out->part_doubles = pd;
@@ -963,11 +944,9 @@ int ensure_fresh(int c_begin, int c_end, cudaStream_t st) {
         }
         const dim3 sgrid((unsigned)ceil_div(P.m, 128), (unsigned)ceil_div(nc, 16));
         if (P.kd == 6)
-            slice_kernel<6><<<sgrid, 128, 0, st>>>(P.X, P.ld, P.m, P.n, c, nc, P.cmax, P.cexp, P.colstore, P.nrc,
-                                                   P.rowstore, P.ncc);
+            slice_kernel<6><<<sgrid, 128, 0, st>>>(P.X, P.ld, P.m, P.n, c, nc, P.cmax, P.cexp, P.colstore, P.nrc);
         else
-            slice_kernel<7><<<sgrid, 128, 0, st>>>(P.X, P.ld, P.m, P.n, c, nc, P.cmax, P.cexp, P.colstore, P.nrc,
-                                                   P.rowstore, P.ncc);
+            slice_kernel<7><<<sgrid, 128, 0, st>>>(P.X, P.ld, P.m, P.n, c, nc, P.cmax, P.cexp, P.colstore, P.nrc);
         g_launch_count += 1;
         for (int k = c; k < e; ++k) { P.fresh[k] = 1; P.cmax_valid[k] = 0; }
         c = e;
@@ -998,16 +977,16 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     P.X = X; P.ld = ld; P.m = m; P.n = n; P.num_sms = num_sms;
     P.fresh.assign((size_t)n, 0);
     P.cmax_valid.assign((size_t)n, 0);
-    // Both stores are zeroed whenever the workspace or the shape changes. The
-    // chunk padding the slicing never writes (rows past m in the last 64-row chunk
-    // of the column store, columns past n in the last 64-column chunk of the row
-    // store) lies inside the TMA boxes and must read as zero, and the rest of the
-    // row store must hold digits or zeros (never bytes of another layout) because
-    // the last K chunk of an update reads columns past K + nc, multiplied by zero
-    // rows of the factor. Repeated runs of one shape keep their zeroed padding.
+    // The store is zeroed whenever the workspace or the shape changes. The chunk
+    // padding the slicing never writes (rows past m in the last 64-row chunk) lies
+    // inside the TMA boxes and must read as zero. The rest must hold digits or
+    // zeros (never bytes of another layout): the last K chunk of an update reads
+    // columns past K + nc, multiplied by zero rows of the factor, and the last row
+    // tile of an update may read the 64-row chunk after the last one (the next
+    // plane's first chunk), whose products land only in rows past m. Repeated runs
+    // of one shape keep their zeroed padding.
     if (P.zeroed_base != (const void*)P.colstore || P.zeroed_m != m || P.zeroed_n != n) {
         cudaError_t ce = (cudaError_t)zero_async(P.colstore, (size_t)KD_MAX * P.nrc * 64 * n * 2, st);
-        if (ce == cudaSuccess) ce = (cudaError_t)zero_async(P.rowstore, (size_t)KD_MAX * P.ncc * 64 * m * 2, st);
         if (ce != cudaSuccess) return (int)ce;
         P.zeroed_base = P.colstore;
         P.zeroed_m = m;
@@ -1018,7 +997,8 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     // Chunked stores as 3-D tensors {64, columns or rows, plane x chunk}.
     int rc = make_map3(&P.map_col_a, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, TILE_M);
     if (!rc) rc = make_map3(&P.map_col_b, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 32);
-    if (!rc) rc = make_map3(&P.map_row_a, P.rowstore, 64, m, KD_MAX * P.ncc, 64, m * 64, TILE_M);
+    // Update A tiles: 64 columns of two adjacent 64-row chunks (128 rows).
+    if (!rc) rc = make_map3(&P.map_col_u, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, KCH, 2);
     if (!rc) rc = make_map3(&P.map_bdig16, P.bdig, P.kpad, 16, KD_MAX, P.kpad, 16 * P.kpad, 16);
     if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
     if (rc) return rc;
@@ -1142,7 +1122,7 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     return launch_gram_reduce(P.part, gp.rc, na, nb, out, ldo, st);
 }
 
-// bdigit + the tensor-core product X[:, c0:c0+nc] = rowstore[:, 0:kin] * Bp, after the
+// bdigit + the tensor-core product X[:, c0:c0+nc] = digits[:, 0:kin] * Bp, after the
 // caller has filled Bp/bmax.
 // Output columns go in groups of at most 32 (one tensor-core pass each). Every
 // group reads the same digit planes of X[:, 0:kin], which were sliced before the
@@ -1164,7 +1144,7 @@ static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int 
         cudaError_t ce = (cudaError_t)zero_async(P.cmax + c0 + j0, (size_t)ng * sizeof(unsigned long long), st);
         if (ce != cudaSuccess) return (int)ce;
         UpdateParams up;
-        up.ncc = (int)P.ncc;
+        up.nrc = (int)P.nrc;
         up.m = m; up.kin = kin; up.nc = ng; up.c0 = c0 + j0; up.ld = ld; up.X = X; up.fexp = P.fexp;
         up.cmax = P.cmax; up.err = P.err; up.tile_ctr = P.tile_ctr;
         ce = (cudaError_t)zero_async(P.tile_ctr, sizeof(int), st);
@@ -1172,7 +1152,7 @@ static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int 
         const int ntiles = (int)ceil_div(m, TILE_M);
         const int grid = ntiles < num_sms ? ntiles : num_sms;
 #define BCGS_UPD(NBT, KDT) \
-        update_tc_kernel<NBT, KDT><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(P.map_row_a, P.map_bdig##NBT, up)
+        update_tc_kernel<NBT, KDT><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(P.map_col_u, P.map_bdig##NBT, up)
         if (NB == 16) {
             if (P.kd == 6) BCGS_UPD(16, 6); else BCGS_UPD(16, 7);
         } else {

@@ -7,7 +7,11 @@
 //     8-row swizzle atom), version 1 and layout type 2 (SWIZZLE_128B); each
 //     16-element K step advances the start address by 32 bytes;
 //   * the instruction descriptor: D = F32 (bits 4-5), A = B = BF16 (bits 7-9,
-//     10-12), K-major A and B, N>>3 at bits 17-22, M>>4 at bits 24-28.
+//     10-12), K-major A and B, N>>3 at bits 17-22, M>>4 at bits 24-28;
+//   * an MN-major A (bit 15 of the instruction descriptor) is a tile whose 128-byte
+//     rows run along M: 8 consecutive K indices form one 1 KB swizzle atom, atoms
+//     along K are SBO = 1024 bytes apart and 64-element blocks along M are LBO
+//     bytes apart; each 16-element K step advances the start address by 2 KB.
 #pragma once
 
 #include <cstdint>
@@ -121,6 +125,23 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
 
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// MN-major 128-byte-swizzled operand: LBO (bits 16-29) = stride between 64-element
+// blocks along M or N, SBO (bits 32-45) = 1024 bytes between 8-row K atoms.
+__device__ __forceinline__ uint64_t sw128_desc_mn(uint32_t saddr, uint32_t lbo_bytes) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo_bytes >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((1024u >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// As idesc_bf16_f32 with A read MN-major (bit 15).
+__host__ __device__ constexpr uint32_t idesc_bf16_f32_amn(int M, int N) {
+    return idesc_bf16_f32(M, N) | (1u << 15);
 }
 
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
