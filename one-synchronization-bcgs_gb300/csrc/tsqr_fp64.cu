@@ -4,10 +4,11 @@
 // call sites :107,:271,:413,:505,:522,:534,:601,:613,:651). Trilinos is not part of
 // the reference, so the algorithm here is the published TSQR reduction tree:
 //
-//   level 0: the panel is cut into tiles of TR rows; one warp per tile computes a
-//            Householder QR of its tile in shared memory (warp butterfly sums, no
-//            block barriers), writes the explicit tile Q in place and its nc x nc
-//            R into the next level's stack.
+//   level 0: the panel is cut into tiles of TR rows; one CTA of 1-4 warps per
+//            tile computes a Householder QR of its tile in shared memory (warp
+//            butterfly sums; the warps share out the columns each reflector is
+//            applied to), writes the explicit tile Q in place and its nc x nc R
+//            into the next level's stack.
 //   level l: the stacked R factors (a (tiles * nc) x nc matrix) are cut into tiles
 //            of TR rows again and factored the same way, until one tile remains.
 //   root   : R is sign-normalized (diag(R) >= 0, the column signs moved into Q).
@@ -22,7 +23,30 @@
 
 namespace bcgs {
 
-int tsqr_tile_rows(int nc) { return nc <= 32 ? 256 : 128; }
+// Tile rows and warps per tile of the single-panel tile kernel by template width.
+// All tiles hold 256 rows (BCGS_TSQR_TR64 for nc > 32). A level of the tree
+// divides the row count by TR / nc, so taller tiles mean fewer levels and fewer
+// flops, at the price of fewer tiles resident per SM. The reflector application
+// is split over W warps by groups of columns. Measured on GB300 at m = 2^23,
+// n = 512 (TSQR of block 1 per BCGSI+P-1S QR): nc = 64 with 256-row tiles and 8
+// warps (one tile per SM) 420 ms; 128-row tiles with 4 warps (three per SM) 632
+// ms, with 8 warps 709 ms; 256-row tiles with 16 warps 465 ms. nc = 32 with 4
+// warps 78.5 ms, 8 warps 91.5 ms. nc = 16 with one warp 17.8 ms, two 18.8 ms.
+#ifndef BCGS_TSQR_TR64
+#define BCGS_TSQR_TR64 256
+#endif
+#ifndef BCGS_TSQR_W64
+#define BCGS_TSQR_W64 8
+#endif
+#ifndef BCGS_TSQR_W32
+#define BCGS_TSQR_W32 4
+#endif
+template <int NC>
+constexpr int tsqr_tr() { return NC <= 32 ? 256 : BCGS_TSQR_TR64; }
+template <int NC>
+constexpr int tsqr_tile_warps() { return NC > 32 ? BCGS_TSQR_W64 : (NC > 16 ? BCGS_TSQR_W32 : 1); }
+
+int tsqr_tile_rows(int nc) { return nc <= 32 ? 256 : BCGS_TSQR_TR64; }
 
 // Shared memory of one tile: the TR x NC tile, column-major (ld TR), and its NC
 // Householder scalars.
@@ -63,7 +87,26 @@ __device__ __forceinline__ void apply_reflector(double* a, int TR, int c0, const
     }
 }
 
-// One warp per tile, the tile in shared memory (lane L owns rows L, L+32, ...).
+template <int W>
+__device__ __forceinline__ void tile_sync() {
+    if (W == 1) __syncwarp(); else __syncthreads();
+}
+
+// Applies the reflector (v, t) to columns [c_begin, nc) of the tile: groups of 4
+// columns q = 0, 1, ... starting at c_begin go to warp q mod W, then the remaining
+// single columns continue the same count. Each column's sum is one warp's
+// butterfly, so the result does not depend on W. Group 0, which holds column
+// c_begin, always belongs to warp 0.
+template <int RPL, int W>
+__device__ __forceinline__ void apply_reflector_cols(double* a, int TR, int c_begin, int nc, const double* v,
+                                                     double t, int lane, int warp) {
+    const int ng = (nc - c_begin) / 4;
+    for (int q = warp; q < ng; q += W) apply_reflector<RPL, 4>(a, TR, c_begin + 4 * q, v, t, lane);
+    for (int c = c_begin + 4 * ng; c < nc; ++c)
+        if ((ng + (c - c_begin - 4 * ng)) % W == warp) apply_reflector<RPL, 1>(a, TR, c, v, t, lane);
+}
+
+// W warps per tile, the tile in shared memory (lane L owns rows L, L+32, ...).
 // A: rows x nc (lda); tile `tile` covers rows [tile*TR, min(rows, (tile+1)*TR)).
 // Householder QR by the conventions of LAPACK's dgeqr2/dlarfg (column j:
 // beta = -sign(alpha) sqrt(alpha^2 + ||x||^2), tau = (beta - alpha)/beta,
@@ -71,26 +114,33 @@ __device__ __forceinline__ void apply_reflector(double* a, int TR, int c0, const
 // [tile*nc, (tile+1)*nc) (ld ldr), then the explicit tile Q formed in place in
 // dorg2r's order (backward over the reflectors) and written to Q (ldq; may alias
 // A). Tiles shorter than nc rows are padded with zero rows; padded rows of Q are
-// not written. Every dot product is a warp butterfly sum, so the result is
-// bit-identical run to run. smem holds tsqr_tile_smem_bytes(TR, NC).
-template <int NC>
+// not written. Every dot product is a warp butterfly sum, and every warp forms
+// the reflector from the same column with the same operations, so the result is
+// bit-identical run to run and for any W. smem holds tsqr_tile_smem_bytes(TR, NC).
+//
+// One barrier per reflector: all warps read column j (the reflector), apply it to
+// their column groups, and meet; then warp 0 stores column j. The next step reads
+// and writes other columns, except in the backward phase, where column j is in
+// group 0 of step j - 1, which warp 0 itself applies.
+template <int NC, int W>
 __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, double* Q, i64 ldq,
                                double* __restrict__ Rst, i64 ldr, i64 tile, double* smem) {
-    constexpr int TR = NC <= 32 ? 256 : 128;
+    constexpr int TR = tsqr_tr<NC>();
     constexpr int RPL = TR / 32;
     double* a = smem;              // a[c * TR + r]
     double* tau = smem + TR * NC;
     const int lane = threadIdx.x & 31;
+    const int warp = W == 1 ? 0 : (int)(threadIdx.x >> 5);
     const i64 row0 = tile * TR;
     const i64 h = min((i64)TR, rows - row0);
-    __syncwarp();
-    for (int c = 0; c < nc; ++c)
+    tile_sync<W>();
+    for (int c = warp; c < nc; c += W)
 #pragma unroll
         for (int i = 0; i < RPL; ++i) {
             const int r = lane + 32 * i;
             a[c * TR + r] = (r < h) ? A[row0 + r + (i64)c * lda] : 0.0;
         }
-    __syncwarp();
+    tile_sync<W>();
 
     for (int j = 0; j < nc; ++j) {
         double v[RPL];
@@ -114,28 +164,25 @@ __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, doubl
             const int r = lane + 32 * i;
             v[i] = (r > j) ? v[i] * scal : (r == j ? 1.0 : 0.0);
         }
-        __syncwarp();
+        if (t != 0.0) apply_reflector_cols<RPL, W>(a, TR, j + 1, nc, v, t, lane, warp);
+        tile_sync<W>();
+        if (warp == 0) {
 #pragma unroll
-        for (int i = 0; i < RPL; ++i) {
-            const int r = lane + 32 * i;
-            if (r > j) a[j * TR + r] = v[i];
-            else if (r == j) a[j * TR + r] = beta;
+            for (int i = 0; i < RPL; ++i) {
+                const int r = lane + 32 * i;
+                if (r > j) a[j * TR + r] = v[i];
+                else if (r == j) a[j * TR + r] = beta;
+            }
+            if (lane == 0) tau[j] = t;
         }
-        if (lane == 0) tau[j] = t;
-        __syncwarp();
-        if (t != 0.0) {
-            int c = j + 1;
-            for (; c + 4 <= nc; c += 4) apply_reflector<RPL, 4>(a, TR, c, v, t, lane);
-            for (; c < nc; ++c) apply_reflector<RPL, 1>(a, TR, c, v, t, lane);
-        }
-        __syncwarp();
     }
+    tile_sync<W>();
     // R to the stack (upper, lower zero).
-    for (int e = lane; e < nc * nc; e += 32) {
+    for (int e = threadIdx.x; e < nc * nc; e += 32 * W) {
         const int i = e % nc, c = e / nc;
         Rst[tile * nc + i + (i64)c * ldr] = (i <= c) ? a[c * TR + i] : 0.0;
     }
-    __syncwarp();
+    tile_sync<W>();
     // Explicit Q in place (dorg2r): for j = nc-1 .. 0, apply H_j to columns j+1..
     // and set column j to (I - tau v v^T) e_j.
     for (int j = nc - 1; j >= 0; --j) {
@@ -146,33 +193,33 @@ __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, doubl
             const int r = lane + 32 * i;
             v[i] = (r > j) ? a[j * TR + r] : (r == j ? 1.0 : 0.0);
         }
-        if (t != 0.0) {
-            int c = j + 1;
-            for (; c + 4 <= nc; c += 4) apply_reflector<RPL, 4>(a, TR, c, v, t, lane);
-            for (; c < nc; ++c) apply_reflector<RPL, 1>(a, TR, c, v, t, lane);
-        }
+        if (t != 0.0) apply_reflector_cols<RPL, W>(a, TR, j + 1, nc, v, t, lane, warp);
+        tile_sync<W>();
+        if (warp == 0) {
 #pragma unroll
-        for (int i = 0; i < RPL; ++i) {
-            const int r = lane + 32 * i;
-            a[j * TR + r] = (r > j) ? -t * v[i] : (r == j ? 1.0 - t : 0.0);
+            for (int i = 0; i < RPL; ++i) {
+                const int r = lane + 32 * i;
+                a[j * TR + r] = (r > j) ? -t * v[i] : (r == j ? 1.0 - t : 0.0);
+            }
+            __syncwarp();
         }
-        __syncwarp();
     }
-    for (int c = 0; c < nc; ++c)
+    tile_sync<W>();
+    for (int c = warp; c < nc; c += W)
 #pragma unroll
         for (int i = 0; i < RPL; ++i) {
             const int r = lane + 32 * i;
             if (r < h) Q[row0 + r + (i64)c * ldq] = a[c * TR + r];
         }
-    __syncwarp();
+    tile_sync<W>();
 }
 
 template <int NC>
-__global__ void __launch_bounds__(32)
+__global__ void __launch_bounds__(32 * tsqr_tile_warps<NC>())
 tsqr_tile_kernel(const double* A, i64 lda, i64 rows, int nc, double* Q, i64 ldq,
                  double* __restrict__ Rst, i64 ldr) {
     extern __shared__ double smem[];
-    tsqr_tile_body<NC>(A, lda, rows, nc, Q, ldq, Rst, ldr, blockIdx.x, smem);
+    tsqr_tile_body<NC, tsqr_tile_warps<NC>()>(A, lda, rows, nc, Q, ldq, Rst, ldr, blockIdx.x, smem);
 }
 
 // Root fix-up: make diag(R) >= 0. R (nc x nc, ld ldr) rows with a negative
@@ -257,7 +304,7 @@ static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR
         tsqr_tile_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (attr_rc != cudaSuccess) return (int)attr_rc;
     // Level matrices: level 0 is the panel itself; level l >= 1 lives in ws.
-    constexpr int kMaxLevels = 48;   // nc > 32 reduces 128 rows to 64 per level: 2^k rows need about k levels
+    constexpr int kMaxLevels = 48;   // each level divides the rows by TR / nc >= 2: 2^k rows need at most k levels
     double* lvl_ptr[kMaxLevels];
     i64 lvl_rows[kMaxLevels], lvl_ld[kMaxLevels];
     lvl_ptr[0] = X + (i64)c0 * ld;
@@ -270,7 +317,7 @@ static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR
         const i64 tiles = ceil_div(lvl_rows[L], TR);
         double* next = cursor;
         cursor += tiles * nc * nc;
-        tsqr_tile_kernel<NC><<<(unsigned)tiles, 32, smem, st>>>(
+        tsqr_tile_kernel<NC><<<(unsigned)tiles, 32 * tsqr_tile_warps<NC>(), smem, st>>>(
             lvl_ptr[L], lvl_ld[L], lvl_rows[L], nc, lvl_ptr[L], lvl_ld[L], next, tiles * nc);
         g_launch_count += 1;
         ++L;
@@ -280,7 +327,7 @@ static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR
     }
     // Root: one tile; its R goes to a small slot after the stacks.
     double* rroot = cursor;
-    tsqr_tile_kernel<NC><<<1, 32, smem, st>>>(lvl_ptr[L], lvl_ld[L], lvl_rows[L], nc, lvl_ptr[L],
+    tsqr_tile_kernel<NC><<<1, 32 * tsqr_tile_warps<NC>(), smem, st>>>(lvl_ptr[L], lvl_ld[L], lvl_rows[L], nc, lvl_ptr[L],
                                               lvl_ld[L], rroot, nc);
     tsqr_root_fix<<<1, 256, 0, st>>>(lvl_ptr[L], lvl_ld[L], (int)lvl_rows[L], nc, rroot, nc, R, ldR);
     g_launch_count += 2;
@@ -316,9 +363,9 @@ tsqr_tile_batched(const TsqrTileJob* __restrict__ jobs, const int* __restrict__ 
     const TsqrTileJob& J = jobs[j];
     const i64 tile = blockIdx.x - prefix[j];
     if (J.nc <= 8)
-        tsqr_tile_body<8>(J.A, J.lda, J.rows, J.nc, J.A, J.lda, J.Rst, J.ldr, tile, smem);
+        tsqr_tile_body<8, 1>(J.A, J.lda, J.rows, J.nc, J.A, J.lda, J.Rst, J.ldr, tile, smem);
     else
-        tsqr_tile_body<16>(J.A, J.lda, J.rows, J.nc, J.A, J.lda, J.Rst, J.ldr, tile, smem);
+        tsqr_tile_body<16, 1>(J.A, J.lda, J.rows, J.nc, J.A, J.lda, J.Rst, J.ldr, tile, smem);
 }
 
 __global__ void tsqr_root_batched(const TsqrRootJob* __restrict__ jobs) {
