@@ -139,16 +139,18 @@ __global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c
 
 // Slice columns [c0, c0+nc) of X into the digit store. A CTA handles 128 rows x
 // 16 columns (grid: row tiles x column groups), one row per thread: 16 coalesced
-// column loads and the digits, staged in shared memory as [plane][column][row],
-// then written per (plane, column) as two 128-byte runs (64 rows each) in 16-byte
-// pieces.
+// column loads and the digits, staged in shared memory as [plane][64-row
+// half][column][64 rows]. That is the store's own layout: for one plane and one
+// 64-row chunk, the 16 columns' runs of 64 rows are one contiguous 2 KB block of
+// HBM. A full tile leaves as 2 KD bulk copies of 2 KB, issued by as many threads.
+// Ragged tiles (rows past m, or fewer than 16 columns) are stored element-wise.
 template <int KD>
 __global__ void __launch_bounds__(128, 6)
 slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
              const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
              unsigned short* __restrict__ colstore, i64 nrc) {
     constexpr int CG = 16;                   // columns per CTA
-    __shared__ __align__(16) unsigned short sdig[KD][CG][128];
+    __shared__ __align__(128) unsigned short sdig[KD][2][CG][64];
     const int t = threadIdx.x;
     const int g = blockIdx.y * CG;           // first column of this group (relative to c0)
     const i64 r0 = (i64)blockIdx.x * 128;
@@ -162,25 +164,33 @@ slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
         int d[KD];
         split_digits<KD>(x[j], g + j < nc ? scale_exp(cmax[c0 + g + j]) : 0, d);
 #pragma unroll
-        for (int i = 0; i < KD; ++i) sdig[i][j][t] = bf16_bits_of_int(d[i]);
+        for (int i = 0; i < KD; ++i) sdig[i][t >> 6][j][t & 63] = bf16_bits_of_int(d[i]);
     }
+    const bool full = (r0 + 128 <= m) && (g + CG <= nc);
+    if (full) tc::fence_proxy_async_smem();
     __syncthreads();
-    const bool full = (r0 + 128 <= m);
-    // Element (r, c) of plane i at ((i*nrc + r/64)*n + c)*64 + r%64; per (plane,
-    // column) the CTA's 128 rows are two 128-byte runs = 16 pieces of 16 bytes.
-    for (int e = t; e < KD * CG * 16; e += 128) {
-        const int piece = e & 15, ij = e >> 4;
-        const int i = ij / CG, j = ij % CG;
-        if (g + j >= nc) continue;
-        const i64 rr = r0 + piece * 8;
-        unsigned short* dst = colstore + (((i64)i * nrc + rr / 64) * n + (c0 + g + j)) * 64 + (rr & 63);
-        const unsigned short* src = &sdig[i][j][piece * 8];
-        if (full) {
-            *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(src);
-        } else {
-            for (int q = 0; q < 8; ++q)
-                if (rr + q < m) dst[q] = src[q];
+    // Element (r, c) of plane i at ((i*nrc + r/64)*n + c)*64 + r%64.
+    if (full) {
+        if (t < 2 * KD) {
+            const int i = t >> 1, h = t & 1;
+            unsigned short* dst = colstore + (((i64)i * nrc + r0 / 64 + h) * n + (c0 + g)) * 64;
+            tc::bulk_store(dst, &sdig[i][h][0][0], CG * 64 * 2);
+            tc::bulk_commit();
+            tc::bulk_wait_read();
         }
+        return;
+    }
+    for (int e = t; e < KD * 2 * CG * 8; e += 128) {
+        const int piece = e & 7, rest = e >> 3;     // 16-byte piece of one 64-row run
+        const int j = rest % CG, ih = rest / CG;
+        const int i = ih >> 1, h = ih & 1;
+        if (g + j >= nc) continue;
+        const i64 rr = r0 + h * 64 + piece * 8;
+        if (rr >= m) continue;
+        unsigned short* dst = colstore + (((i64)i * nrc + rr / 64) * n + (c0 + g + j)) * 64 + (rr & 63);
+        const unsigned short* src = &sdig[i][h][j][piece * 8];
+        for (int q = 0; q < 8; ++q)
+            if (rr + q < m) dst[q] = src[q];
     }
 }
 

@@ -92,6 +92,21 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
+// Bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) from
+// this CTA's shared memory to global memory, in the calling thread's bulk group.
+__device__ __forceinline__ void bulk_store(void* gdst, const void* ssrc, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(smem_u32(ssrc)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// Waits until the calling thread's bulk copies have finished reading shared memory.
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// Orders this thread's ordinary shared-memory writes before later bulk copies that read them.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // 3-D TMA tile load multicast to the CTAs of this cluster in `mask`: the tile lands
 // at the same shared-memory offset `dst` in each, and completes bytes on the
 // barrier at offset `bar` in each.
