@@ -131,6 +131,34 @@ def test_device_entry_point_matches_host(lib):
     assert np.array_equal(np.triu(Rd), np.triu(Rh))
 
 
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_host_path_timeline(lib, precision):
+    """orth.h host-buffer runs overlap the copies with the QR and record a timeline:
+    X is resident before the kernels finish, Q is back after them, and the call's
+    wall time covers all three. The result equals the device entry point's."""
+    torch = pytest.importorskip("torch")
+    m, n, s = 300000, 128, 16
+    X = inputs.graded_host(m, n, 1e4, seed=11)
+    prec = orth.FP64 if precision == "fp64" else orth.SPLIT_BF16
+    assert orth.set_host_precision(prec) == 0
+    try:
+        Qh, Rh, rc, st = orth.qr("bcgsi2P1s", X, s)
+    finally:
+        orth.set_host_precision(orth.FP64)
+    assert rc == 0 and st["breakdown_step"] == 0
+    t = orth.last_host_timing()
+    assert 0.0 < t["x_resident_ms"] <= t["compute_done_ms"] + 1e-3, t
+    assert t["compute_done_ms"] <= t["q_back_ms"] + 1e-3, t
+    assert t["q_back_ms"] <= t["wall_ms"] + 1.0, t
+    dX = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
+    dR = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    rc, _ = orth.run_dev("bcgsi2P1s", m, n, s, dX.data_ptr(), m, dR.data_ptr(), n, prec,
+                         torch.cuda.current_stream().cuda_stream)
+    assert rc == 0
+    assert np.array_equal(dX.cpu().numpy().T, Qh)
+    assert np.array_equal(np.triu(dR.cpu().numpy().T), np.triu(Rh))
+
+
 def test_large_properties_fp64(lib):
     """Size-independent properties at m = 2^20: orthogonality and residual."""
     torch = pytest.importorskip("torch")
