@@ -43,6 +43,6 @@ def qr_tolerance(cond: float) -> float:
 
 
 def metric_ok(ours: float, ref: float, floor: float) -> bool:
-    """The spec parity rule: within 10x of the reference's value, with an
+    """The parity rule: within 10x of the reference's value, with an
     absolute floor at the unit-roundoff level."""
     return np.isfinite(ours) and ours <= 10.0 * max(ref, floor)

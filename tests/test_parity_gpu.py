@@ -5,7 +5,7 @@ device-pointer entry point). The oracle is the reference's own output (golden
 fixtures made by oracle/_ref) and the numpy restatement (oracle/bcgs_port.py).
 Tolerances: Q and R/||R|| entries within 200*u*cond(X) + 1e-13 after sign
 normalization; LOO and relative residual within 10x of the reference's (with an
-n*u floor), the spec parity rule.
+n*u floor), the parity rule.
 """
 import numpy as np
 import pytest

@@ -5,7 +5,7 @@ operand (48-bit fixed point per column), so its products match FP64 to about
 2^-47 relative to the operand norms. Checked here through the C ABI:
   * the tall Gram primitive against the FP64 Gram on ragged shapes;
   * full QRs of every variant: LOO_2 <= 1e-12 and relative residual <= 1e-13
-    (the north-star split-precision gate) and agreement with the FP64 path;
+    (the split-precision accuracy target) and agreement with the FP64 path;
   * bit-exact results run to run.
 """
 import numpy as np
@@ -72,7 +72,7 @@ def test_split_qr_accuracy(lib, variant, kappa, mode):
         assert loo <= 10 * max(loo_f, 1e-15), (loo, loo_f)
         assert res <= 10 * max(res_f, 1e-15), (res, res_f)
     else:
-        # 48-bit digits: the spec gate LOO <= 1e-12, except where the variant
+        # 48-bit digits: the accuracy target LOO <= 1e-12, except where the variant
         # itself loses orthogonality in FP64 (bcgsi21s at high kappa).
         assert loo <= max(1e-12, 200 * loo_f), (loo, loo_f)
         assert res <= 1e-12, res
