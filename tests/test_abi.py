@@ -65,3 +65,23 @@ def test_sync_counts(lib):
 
 def test_version(lib):
     assert "sm_103a" in orth.version()
+
+
+def test_host_timing_is_zero_before_any_host_run(lib):
+    # The timeline is per thread and set only by a successful host-buffer run; a
+    # fresh thread reads zeros without touching the GPU.
+    import threading
+    got = {}
+    t = threading.Thread(target=lambda: got.update(orth.last_host_timing()))
+    t.start()
+    t.join()
+    assert got == {"x_resident_ms": 0.0, "compute_done_ms": 0.0, "q_back_ms": 0.0, "wall_ms": 0.0}
+
+
+def test_split_shape_support(lib):
+    # Split precision takes s <= 64 with n >= 2s and at least one 128-row tile.
+    assert orth.split_supported(1 << 20, 512, 16)
+    assert orth.split_supported(1 << 20, 512, 64)
+    assert not orth.split_supported(1 << 20, 512, 65)
+    assert not orth.split_supported(1 << 20, 100, 64)
+    assert not orth.split_supported(127, 32, 4)
