@@ -161,6 +161,14 @@ void orth_gb300_batch_destroy(orth_gb300_batch *plan);
  * for these shapes would hold. */
 int orth_gb300_batch_dry_run(int count, const int *m, const int *n, const int *s, long long *stages,
                              long long *launches_per_run, long long *workspace_bytes);
+/* The schedule of a split-precision batch without a GPU: returns the number of
+ * scratch slots S a run would use when free_bytes of device memory are free
+ * (free_bytes < 0: no memory limit; max_slots >= 1 caps S), and fills slot_of[b]
+ * (the slot of matrix b) and order[b] (the b-th matrix enqueued: longest job
+ * m n^2 first, each to the least loaded slot). Either array may be NULL. 0 for
+ * invalid arguments. */
+int orth_gb300_split_batch_plan(int count, const int *m, const int *n, const int *s, long long free_bytes,
+                                int max_slots, int *slot_of, int *order);
 
 /*
  * Diagnostic: fill every SM's shared memory with the 64-bit pattern `bits` (e.g. a

@@ -111,6 +111,9 @@ def load(path: str | None = None):
     lib.orth_gb300_batch_destroy.restype = None
     lib.orth_gb300_batch_dry_run.argtypes = [ctypes.c_int, P_int, P_int, P_int, P_ll, P_ll, P_ll]
     lib.orth_gb300_batch_dry_run.restype = ctypes.c_int
+    lib.orth_gb300_split_batch_plan.argtypes = [ctypes.c_int, P_int, P_int, P_int, ctypes.c_longlong, ctypes.c_int,
+                                                P_int, P_int]
+    lib.orth_gb300_split_batch_plan.restype = ctypes.c_int
     lib.orth_gb300_reserve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.orth_gb300_reserve.restype = ctypes.c_int
     lib.orth_gb300_release.argtypes = []
@@ -257,6 +260,17 @@ def batch_dry_run(ms, ns, ss) -> dict:
     rc = int(load().orth_gb300_batch_dry_run(len(ms), _int_array(ms), _int_array(ns), _int_array(ss),
                                              ctypes.byref(st), ctypes.byref(la), ctypes.byref(wb)))
     return {"rc": rc, "stages": st.value, "launches": la.value, "bytes": wb.value}
+
+
+def split_batch_plan(ms, ns, ss, free_bytes: int = -1, max_slots: int = 0) -> dict:
+    """Slot count, slot of each matrix and enqueue order of a split-precision batch
+    (orth_gb300_split_batch_plan; no GPU needed)."""
+    c = len(ms)
+    slot = (ctypes.c_int * c)()
+    order = (ctypes.c_int * c)()
+    S = int(load().orth_gb300_split_batch_plan(c, _int_array(ms), _int_array(ns), _int_array(ss), int(free_bytes),
+                                            int(max_slots), slot, order))
+    return {"slots": S, "slot_of": list(slot), "order": list(order)}
 
 
 class Batch:

@@ -819,43 +819,35 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
 
 }  // namespace
 
-// Split-precision batches: the matrices one after another on `st` through the
-// single-matrix driver (its digit store is 14 bytes per element, so a whole
-// batch's stores at once would not fit). Workspaces are grown for the largest
-// shapes first, so no allocation happens between matrices. After each matrix its
-// status words (4 ints) and the split kernels' error word go to dstatus[8 b ..]
-// on the device; nothing waits on the host.
-int split_batch_enqueue(int variant, int count, const int* m, const int* n, const int* s, double* const* dX,
-                        const long long* ldX, double* const* dR, const int* ldR, int precision, cudaStream_t st,
-                        int* dstatus, int max_slots) {
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (init_ctx()) return 3;
+// Schedule of a split-precision batch (host arithmetic only): the number of
+// scratch slots S and each matrix's slot. A slot's scratch is sized for its
+// largest matrix, and the longest-first assignment gives each slot one of the S
+// largest, so S is the most slots whose S largest workspaces fit in half of
+// free_bytes (at least one; free_bytes < 0: no memory limit), at most kSlots,
+// count and max_slots (if >= 1). Jobs (weight m n^2) go longest first, each to the
+// least loaded slot; `order` receives that sequence.
+int split_batch_plan(int count, const int* m, const int* n, const int* s, int num_sms, long long free_bytes,
+                     int max_slots, std::vector<int>& order, std::vector<int>& slot_of) {
+    order.assign((size_t)(count > 0 ? count : 0), 0);
+    slot_of.assign(order.size(), 0);
+    if (count < 1) return 0;
     int S = count < kSlots ? count : kSlots;
     if (max_slots >= 1 && S > max_slots) S = max_slots;
-    {
-        // Each slot's scratch is sized for its largest matrix, and the longest-first
-        // assignment gives each slot one of the S largest. Take the most slots whose
-        // S largest workspaces fit in half of the free device memory (at least one).
+    if (free_bytes >= 0) {
         std::vector<double> wsz(count);
         for (int b = 0; b < count; ++b)
-            wsz[b] = (double)split_workspace_bytes(m[b], n[b], s[b], g_ctx.num_sms) +
-                     8.0 * ((double)part_doubles(m[b], n[b], s[b], g_ctx.num_sms) +
-                            (double)tsqr_workspace_doubles(m[b], s[b]));
+            wsz[b] = (double)split_workspace_bytes(m[b], n[b], s[b], num_sms) +
+                     8.0 * ((double)part_doubles(m[b], n[b], s[b], num_sms) + (double)tsqr_workspace_doubles(m[b], s[b]));
         std::sort(wsz.begin(), wsz.end(), [](double a, double b) { return a > b; });
-        size_t free_b = 0, total_b = 0;
-        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
-            double acc = 0.0;
-            int fit = 0;
-            for (int k = 0; k < S; ++k) {
-                acc += wsz[k];
-                if (acc > 0.5 * (double)free_b) break;
-                fit = k + 1;
-            }
-            S = fit > 1 ? fit : 1;
+        double acc = 0.0;
+        int fit = 0;
+        for (int k = 0; k < S; ++k) {
+            acc += wsz[k];
+            if (acc > 0.5 * (double)free_bytes) break;
+            fit = k + 1;
         }
+        S = fit > 1 ? fit : 1;
     }
-    // Longest job (m n^2) first, each to the least loaded slot.
-    std::vector<int> order(count), slot_of(count);
     for (int b = 0; b < count; ++b) order[b] = b;
     std::sort(order.begin(), order.end(), [&](int a, int b) {
         const double wa = (double)m[a] * n[a] * n[a], wb = (double)m[b] * n[b] * n[b];
@@ -869,6 +861,24 @@ int split_batch_enqueue(int variant, int count, const int* m, const int* n, cons
         slot_of[b] = k;
         load[k] += (double)m[b] * n[b] * n[b];
     }
+    return S;
+}
+
+// Split-precision batches: the matrices one after another on `st` through the
+// single-matrix driver (its digit store is 14 bytes per element, so a whole
+// batch's stores at once would not fit). Workspaces are grown for the largest
+// shapes first, so no allocation happens between matrices. After each matrix its
+// status words (4 ints) and the split kernels' error word go to dstatus[8 b ..]
+// on the device; nothing waits on the host.
+int split_batch_enqueue(int variant, int count, const int* m, const int* n, const int* s, double* const* dX,
+                        const long long* ldX, double* const* dR, const int* ldR, int precision, cudaStream_t st,
+                        int* dstatus, int max_slots) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (init_ctx()) return 3;
+    size_t free_b = 0, total_b = 0;
+    const long long fb = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess ? (long long)free_b : -1;
+    std::vector<int> order, slot_of;
+    const int S = split_batch_plan(count, m, n, s, g_ctx.num_sms, fb, max_slots, order, slot_of);
     int rc = 0;
     for (int k = 0; k < S && !rc; ++k)
         if (!g_ctx.slot_stream[k] &&
@@ -995,6 +1005,18 @@ int orth_gb300_gram_dev(int m, int na, int b0, int nb, const double* dX, long lo
         }
     }
     return rc ? 3 : 0;
+}
+
+int orth_gb300_split_batch_plan(int count, const int* m, const int* n, const int* s, long long free_bytes,
+                                int max_slots, int* slot_of, int* order) {
+    if (count < 1 || !m || !n || !s) return 0;
+    std::vector<int> ord, slot;
+    const int S = split_batch_plan(count, m, n, s, kNumSMsDefault, free_bytes, max_slots, ord, slot);
+    for (int b = 0; b < count; ++b) {
+        if (slot_of) slot_of[b] = slot[b];
+        if (order) order[b] = ord[b];
+    }
+    return S;
 }
 
 void orth_gb300_set_gram_chunk_rows(long long rows) {

@@ -62,3 +62,43 @@ def test_dry_run_config4_size(lib):
 ])
 def test_dry_run_rejects(lib, bad):
     assert orth.batch_dry_run(*bad)["rc"] == 2
+
+
+def _config4_shapes(seed=2024, B=4096):
+    rng = np.random.default_rng(seed)
+    m = np.exp(rng.uniform(np.log(2000), np.log(200000), B)).astype(int)
+    s = rng.choice([4, 8, 16], B)
+    p = rng.integers(2, 17, B)
+    return m.tolist(), (s * p).tolist(), s.tolist()
+
+
+def test_split_batch_plan_longest_first_to_least_loaded(lib):
+    ms, ns, ss = _config4_shapes()
+    d = orth.split_batch_plan(ms, ns, ss, free_bytes=270 << 30)
+    S, slot_of, order = d["slots"], d["slot_of"], d["order"]
+    assert S == 16
+    w = [m * n * n for m, n in zip(ms, ns)]
+    # The enqueue order is by job weight m n^2, longest first, ties by index.
+    assert sorted(order) == list(range(len(ms)))
+    assert all((w[a], -a) >= (w[b], -b) for a, b in zip(order, order[1:]))
+    # Replaying the order: every job goes to a least-loaded slot (lowest index on ties).
+    load = [0] * S
+    for b in order:
+        k = min(range(S), key=lambda q: (load[q], q))
+        assert slot_of[b] == k
+        load[k] += w[b]
+    # Longest-processing-time bound: the slots differ by at most the largest job.
+    assert max(load) - min(load) <= max(w)
+
+
+def test_split_batch_plan_fits_free_memory_and_caps(lib):
+    ms, ns, ss = _config4_shapes()
+    assert orth.split_batch_plan(ms, ns, ss, free_bytes=2 << 30)["slots"] == 1
+    few = orth.split_batch_plan(ms, ns, ss, free_bytes=12 << 30)["slots"]
+    assert 1 <= few < 16
+    assert orth.split_batch_plan(ms, ns, ss, free_bytes=-1)["slots"] == 16      # no memory limit
+    one = orth.split_batch_plan(ms, ns, ss, free_bytes=270 << 30, max_slots=1)
+    assert one["slots"] == 1 and set(one["slot_of"]) == {0}
+    three = orth.split_batch_plan(ms[:3], ns[:3], ss[:3])
+    assert three["slots"] == 3 and sorted(three["slot_of"]) == [0, 1, 2]
+    assert orth.split_batch_plan([], [], [])["slots"] == 0
