@@ -363,10 +363,26 @@ bdigit_kernel(const double* __restrict__ Bp, int ldb, int K, int nc, int NB, int
 struct Ring {
     int slot = 0;
     uint32_t phase = 0;
+    uint32_t used = 0;   // slots advanced past so far
     __device__ __forceinline__ void advance(int R) {
+        ++used;
         if (++slot == R) { slot = 0; phase ^= 1u; }
     }
 };
+
+// After an abort, the producer waits (20 ms at most per slot) until the loads of
+// the ring slots it armed most recently have landed, so that no copy is still
+// writing this CTA's shared memory when it exits. The most recent arming of each
+// slot is the one whose phase may still be open.
+__device__ __forceinline__ void drain_ring(uint64_t* full, int R, const Ring& r) {
+    int slot = r.slot;
+    uint32_t phase = r.phase;
+    const uint32_t armed = r.used < (uint32_t)R ? r.used : (uint32_t)R;
+    for (uint32_t i = 0; i < armed; ++i) {
+        if (--slot < 0) { slot = R - 1; phase ^= 1u; }
+        tc::mbar_wait_for(&full[slot], phase, 20000000ULL);
+    }
+}
 
 template <int NB, int KD>
 struct SmemLayout {
@@ -604,6 +620,10 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
                 if (!produce_chunk<NB, KD>(&mapA, &mapB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag, p.err, cs,
                                            rank))
                     break;
+            if (abort_flag) {
+                drain_ring(bars->a_full, RA, ra);
+                drain_ring(bars->b_full, RB, rb);
+            }
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -734,6 +754,10 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
                 if (tile >= ntiles) break;
                 for (int ch = 0; ch < nchunks && ok; ++ch)
                     ok = produce_chunk<NB, KD>(&mapA, &mapB, sA, sB, bars, ra, rb, coords, tile, ch, &abort_flag, p.err);
+            }
+            if (abort_flag) {
+                drain_ring(bars->a_full, RA, ra);
+                drain_ring(bars->b_full, RB, rb);
             }
         }
     } else if (warp == 1) {
