@@ -177,6 +177,15 @@ int orth_gb300_split_batch_plan(int count, const int *m, const int *n, const int
  */
 int orth_gb300_poison_shared_memory(unsigned long long bits, void *stream);
 
+/*
+ * Diagnostic of the failure path: one GPU thread waits, with the bounded wait of
+ * the tensor-core kernels (2 s), on an mbarrier that nothing completes. The wait
+ * gives up, records `code` (nonzero) and sets its abort flag; the kernel returns.
+ * out[0] receives the recorded code (-1 if the wait had succeeded), out[1] the
+ * abort flag. Synchronizes the stream. 0, 2 (invalid arguments) or 3.
+ */
+int orth_gb300_timeout_probe(int code, void *stream, int out[2]);
+
 /* Status of the last run through the orth.h entry points on this thread. */
 void orth_gb300_last_status(orth_gb300_status *status);
 

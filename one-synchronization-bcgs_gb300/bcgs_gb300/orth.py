@@ -95,6 +95,8 @@ def load(path: str | None = None):
     lib.orth_gb300_set_gram_chunk_rows.argtypes = [ctypes.c_longlong]
     lib.orth_gb300_poison_shared_memory.argtypes = [ctypes.c_ulonglong, ctypes.c_void_p]
     lib.orth_gb300_poison_shared_memory.restype = ctypes.c_int
+    lib.orth_gb300_timeout_probe.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+    lib.orth_gb300_timeout_probe.restype = ctypes.c_int
     lib.orth_gb300_set_gram_chunk_rows.restype = None
     P_int, P_ll, P_vp = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_void_p)
     lib.orth_gb300_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, P_int, P_int,
@@ -162,6 +164,14 @@ def last_status() -> dict:
     st = Status()
     load().orth_gb300_last_status(ctypes.byref(st))
     return st.as_dict()
+
+
+def timeout_probe(code: int, stream: int = 0):
+    """Makes one bounded device wait run out (orth_gb300_timeout_probe): returns
+    (rc, recorded code, abort flag)."""
+    out = (ctypes.c_int * 2)()
+    rc = int(load().orth_gb300_timeout_probe(code, ctypes.c_void_p(stream), out))
+    return rc, out[0], out[1]
 
 
 def last_host_timing() -> dict:

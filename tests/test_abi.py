@@ -85,3 +85,8 @@ def test_split_shape_support(lib):
     assert not orth.split_supported(1 << 20, 512, 65)
     assert not orth.split_supported(1 << 20, 100, 64)
     assert not orth.split_supported(127, 32, 4)
+
+
+def test_timeout_probe_rejects_code_zero(lib):
+    # Code 0 means "no error" and is rejected before any CUDA call.
+    assert orth.timeout_probe(0)[0] == 2
