@@ -131,6 +131,30 @@ def test_device_entry_point_matches_host(lib):
     assert np.array_equal(np.triu(Rd), np.triu(Rh))
 
 
+@pytest.mark.parametrize("variant,precision", [("bcgsi2P1s", "fp64"), ("bcgsi2", "fp64"),
+                                               ("bcgsi2P1s", "split"), ("bcgsi21s", "split")])
+def test_device_leading_dimension(lib, variant, precision):
+    """Device buffers with ldX > m (the reference's ldXsub >= msub): the same bits
+    as with tight storage, and the padding rows keep their sentinel."""
+    torch = pytest.importorskip("torch")
+    m, n, s, pad = 30000, 64, 16, 37
+    X = inputs.graded_host(m, n, 1e5, seed=21)
+    prec = orth.FP64 if precision == "fp64" else orth.SPLIT_BF16
+    st = torch.cuda.current_stream().cuda_stream
+    tight = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
+    wide = torch.full((n, m + pad), 7.0, dtype=torch.float64, device="cuda")
+    wide[:, :m] = tight
+    outs = []
+    for buf, ld in ((tight, m), (wide, m + pad)):
+        R = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        rc, status = orth.run_dev(variant, m, n, s, buf.data_ptr(), ld, R.data_ptr(), n, prec, st)
+        assert rc == 0 and status["breakdown_step"] == 0 and status["timeout"] == 0, (rc, status)
+        outs.append(R.cpu().numpy())
+    assert torch.equal(wide[:, :m], tight)
+    assert bool((wide[:, m:] == 7.0).all())
+    assert np.array_equal(np.triu(outs[0].T), np.triu(outs[1].T))
+
+
 @pytest.mark.parametrize("precision", ["fp64", "split"])
 def test_host_path_timeline(lib, precision):
     """orth.h host-buffer runs overlap the copies with the QR and record a timeline:
