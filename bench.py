@@ -64,8 +64,10 @@ def parse():
     ap.add_argument("--fast-steps", type=int, default=1,
                     help="timed 48-bit split QRs reported beside the 56-bit split run")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-rows", type=int, default=1 << 19,
-                    help="rows of the bounded CPU sample (time scaled to m)")
+    ap.add_argument("--cpu-rows", type=int, default=1 << 21,
+                    help="rows of the bounded CPU sample of the cpu_baseline leg (time scaled to m)")
+    ap.add_argument("--ref-budget-s", type=float, default=180.0,
+                    help="--impl reference: wall-time budget of the timed full-size steps")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
@@ -180,8 +182,10 @@ def alg_flops_p1s(m: int, n: int, s: int) -> float:
 
 
 def traffic_ratio(kernel_class: str):
-    """DRAM traffic / algorithmic bytes of a kernel class, from the committed ncu
-    summary (profiles/traffic.json), or None when no capture has been summarized."""
+    """ncu DRAM bytes / traffic bytes (the bytes the kernels as built move at
+    least) of a kernel class, from the committed ncu summary
+    (profiles/traffic.json), or None when no capture of the current kernel has
+    been summarized."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(p):
         return None
@@ -192,39 +196,92 @@ def traffic_ratio(kernel_class: str):
         return None
 
 
-def cpu_sample(args, rows: int):
-    """Time the oracle (numpy/OpenBLAS restatement of the reference) on `rows`
-    rows of the same workload; return seconds and thread count."""
+def host_input(m: int, n: int, kappa: float, seed: int):
+    """The bench's input X (m x n, column-major float64) on the host: built on the
+    GPU by the same seeded construction as the timed arm when one is present
+    (torch only; none of this library's kernels), else by numpy."""
+    from bcgs_gb300 import inputs
+    try:
+        import torch
+        if torch.cuda.is_available():
+            Xt = inputs.graded_device(m, n, kappa, seed=seed, device="cuda")
+            Xh = Xt.cpu().numpy()          # (n, m) row-major == X column-major
+            del Xt
+            torch.cuda.empty_cache()
+            return Xh.T
+    except ImportError:
+        pass
+    return inputs.graded_host(m, n, kappa, seed=seed)
+
+
+def port_step(variant: str, X0, n: int, s: int, work=None):
+    """One QR by the oracle (numpy/OpenBLAS restatement of the reference) on a
+    working copy of X0; returns the seconds of the QR itself. The copy into the
+    preallocated working buffer is outside the interval, as the reference's own
+    driver factors X in place (TESTS/test_orth.c:46-52)."""
+    import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import bcgs_port
-    from bcgs_gb300 import inputs
-    X = inputs.graded_host(rows, args.n, args.kappa, seed=1)
+    m = X0.shape[0]
+    ncols = max(n + s, 3 * s)
+    if work is None or work.shape != (m, ncols):
+        work = np.zeros((m, ncols), order="F")
+    work[:, :n] = X0
+    R = np.zeros((n, n), order="F")
     t0 = time.perf_counter()
-    bcgs_port.run_variant(args.variant, X, args.n, args.s)
-    dt = time.perf_counter() - t0
+    bcgs_port.VARIANTS[variant](work, n, s, R)
+    return time.perf_counter() - t0, work
+
+
+def cpu_sample(args, rows: int):
+    """Time the oracle on the first `rows` rows' worth of the same workload (a
+    bounded sample); return seconds and thread count."""
+    X = host_input(rows, args.n, args.kappa, seed=1234)
+    dt, _ = port_step(args.variant, X, args.n, args.s)
     return dt, os.cpu_count()
 
 
 def run_reference(args, rank, world):
+    """The reference's algorithm on the host cores, at the full workload.
+
+    The reference's own build needs its sources and an x86 OpenBLAS, so the
+    oracle restatement (pinned to that build by the tests) runs here with
+    OpenBLAS on every host thread. Each timed step is one full-size QR (about
+    46 s on 16 Grace cores at m = 2^23), so the steps run are bounded by
+    --ref-budget-s: the line reports how many ran. The warm-up is one QR of a
+    2^16-row sample (thread pools, first-touch of the library)."""
     if rank != 0:
         return
-    steps = []
-    for _ in range(max(0, args.warmup)):
-        pass  # one sample per step is already a few seconds of CPU work
-    threads = os.cpu_count()
+    m, n, s = args.m, args.n, args.s
+    t_gen = time.perf_counter()
+    X0 = host_input(m, n, args.kappa, seed=1234)
+    t_gen = time.perf_counter() - t_gen
+    warm = 0
+    if args.warmup > 0:
+        Xs = X0[: min(m, 1 << 16), :].copy(order="F")
+        port_step(args.variant, Xs, n, s)
+        warm = 1
+        del Xs
+    steps, work = [], None
+    t_start = time.perf_counter()
     for _ in range(max(1, args.steps)):
-        dt, threads = cpu_sample(args, args.cpu_rows)
-        steps.append(dt * args.m / args.cpu_rows * 1e3)
-    ms = sum(steps) / len(steps)
-    sample = (f"{args.variant} on {args.cpu_rows} rows x n={args.n}, s={args.s} (numpy/OpenBLAS "
-              f"restatement of the reference, {threads} threads), time scaled by m/{args.cpu_rows}")
+        dt, work = port_step(args.variant, X0, n, s, work)
+        steps.append(dt)
+        if time.perf_counter() - t_start + dt > args.ref_budget_s:
+            break
+    ms = sum(steps) / len(steps) * 1e3
+    threads = os.cpu_count()
+    sample = (f"{len(steps)} full-size {args.variant} QRs of m={m} x n={n}, s={s} by the numpy/OpenBLAS "
+              f"restatement of the reference on {threads} host threads (steps bounded by a "
+              f"{args.ref_budget_s:.0f} s budget; warm-up: one QR of a 2^16-row sample)")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms",
-        "n_gpus": args.gpus, "steps": len(steps), "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "n_gpus": args.gpus, "steps": len(steps), "steps_requested": args.steps, "warmup": warm,
+        "ms_per_step": round(ms, 3), "step_ms": [round(x * 1e3, 1) for x in steps],
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"{args.variant} QR m={args.m} n={args.n} s={args.s} "
-                               f"kappa={args.kappa:g}"},
+        "config": {"workload": f"{args.variant} QR m={m} n={n} s={s} kappa={args.kappa:g} "
+                               f"(graded X = U diag(sigma) W^T)", "input_build_s": round(t_gen, 1)},
         "cpu_baseline": {"value": round(ms, 3), "unit": "ms", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": round(ms, 3), "unit": "ms", "h2d_bytes_per_step": 0,
@@ -362,10 +419,13 @@ def run_ours(args, rank, world, local_rank):
     if prec != orth.FP64 and args.fast_steps > 0:
         fast_ms, fast_acc = side_leg(orth.SPLIT_BF16_FAST, args.fast_steps)
 
-    # Roofline of the dominant kernel class.
+    # Roofline of the dominant kernel class, on algorithmic bytes (or flops).
+    bytes_alg = alg_bytes_p1s(m, n, s)
+    flops_alg = alg_flops_p1s(m, n, s)
     dom = max(("gram", "update"), key=lambda c: prof[c]["ms"])
     pc = prof[dom]
-    launches = max(1, pc["launches"])
+    calls = max(1, pc["calls"])
+    launch_ms = pc["ms"] / calls
     if prec == orth.FP64:
         peak = orth.fp64_peak_tflops()
         achieved = pc["flops"] / (pc["ms"] * 1e-3) / 1e12 if pc["ms"] > 0 else 0.0
@@ -373,26 +433,44 @@ def run_ours(args, rank, world, local_rank):
                 "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
                 "traffic": None, "kernel": dom,
                 "peak_source": "live DFMA probe (orth_gb300_fp64_peak_probe); MEASURED_PEAKS.json has no FP64 figure",
-                "launch_ms": round(pc["ms"] / launches, 4)}
+                "launch_ms": round(launch_ms, 4),
+                "flops_per_launch": round(pc["flops"] / calls),
+                "whole_qr": {"achieved": round(flops_alg / (ms * 1e-3) / 1e12, 4), "unit": "TFLOP/s",
+                             "frac": round(flops_alg / (ms * 1e-3) / 1e12 / peak, 4) if peak else None}}
     else:
-        mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
-        peaks = json.load(open(mp)) if os.path.exists(mp) else {}
-        peak = peaks.get("hbm_gbs", 6800.0)
-        achieved = pc["bytes"] / (pc["ms"] * 1e-3) / 1e9 if pc["ms"] > 0 else 0.0
+        peak = measured_peak("hbm_gbs")
+        peak_src = "MEASURED_PEAKS.json hbm_gbs (of measured)"
+        if peak is None:
+            peak, peak_src = 6800.0, "fallback 6.8 TB/s (of fallback)"
+        secs = pc["ms"] * 1e-3
+        achieved = pc["bytes"] / secs / 1e9 if secs > 0 else 0.0
+        rate = pc["traffic"] / secs / 1e9 if secs > 0 else 0.0
         kd = 7
-        tensor_tflops = pc["flops"] * kd * (kd + 1) / 2 / (pc["ms"] * 1e-3) / 1e12 if pc["ms"] > 0 else 0.0
+        tensor_tflops = pc["flops"] * kd * (kd + 1) / 2 / secs / 1e12 if secs > 0 else 0.0
         ratio = traffic_ratio(dom)
+        bf16 = measured_peak("bf16_tflops") or 1900.0
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4),
-                "traffic": round(ratio * pc["bytes"] / launches) if ratio is not None else None,
-                "traffic_note": "bytes per launch = ncu DRAM/algorithmic ratio (profiles/traffic.json) x algorithmic bytes per launch",
+                "traffic": round(ratio * pc["traffic"] / calls) if ratio is not None else None,
                 "kernel": {"gram": "gram_tc_kernel<7> + gram_reduce",
                            "update": "bbuild_fused + bdigit + update_tc_kernel<32,7> (fused Q_k/U_k+1 pass)"}[dom],
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
-                "launch_ms": round(pc["ms"] / launches, 4),
-                "bytes_per_launch": round(pc["bytes"] / launches),
+                "peak_source": peak_src,
+                "launch_ms": round(launch_ms, 4),
+                "bytes_per_launch": round(pc["bytes"] / calls),
+                "bytes_note": "algorithmic: 8 B per element of each operand column read once and each column "
+                              "written (FP64-equivalent), per launch of the class's primitive",
+                "traffic_rate": {"value": round(rate, 1), "unit": "GB/s", "frac": round(rate / peak, 4),
+                                 "bytes_per_launch": round(pc["traffic"] / calls),
+                                 "note": "the bytes the kernels as built move: 14 B per element of the BF16 "
+                                         "digit planes read, 8 B per FP64 element written"},
+                "traffic_note": "DRAM bytes per launch = ncu dram bytes / traffic bytes (profiles/traffic.json) "
+                                "x traffic bytes per launch",
                 "tensor_tflops_bf16": round(tensor_tflops, 1),
-                "tensor_frac_of_bf16_peak": round(tensor_tflops / peaks.get("bf16_tflops", 1900.0), 4)}
+                "tensor_frac_of_bf16_peak": round(tensor_tflops / bf16, 4),
+                "whole_qr": {"achieved": round(bytes_alg / (ms * 1e-3) / 1e9, 1), "unit": "GB/s",
+                             "frac": round(bytes_alg / (ms * 1e-3) / 1e9 / peak, 4),
+                             "bytes": bytes_alg,
+                             "note": "8 m [s P (P-1)/2 + 4 n] per BCGSI+P-1S QR"}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -402,8 +480,6 @@ def run_ours(args, rank, world, local_rank):
                "sample": f"{variant} on {args.cpu_rows} rows x n={n}, s={s} with the numpy/OpenBLAS "
                          f"restatement of the reference; time scaled by m/{args.cpu_rows}"}
 
-    bytes_alg = alg_bytes_p1s(m, n, s)
-    flops_alg = alg_flops_p1s(m, n, s)
     line = {
         "metric": METRIC, "value": round(ms, 3), "unit": "ms", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
@@ -423,7 +499,8 @@ def run_ours(args, rank, world, local_rank):
         "split_fast_accuracy": fast_acc,
         "speedup_vs_fp64_gpu": round(fp64_ms / ms, 2) if fp64_ms else None,
         "gpu_launches": int(launches_per_qr * args.steps),
-        "kernel_profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"]} for k, v in prof.items()},
+        "kernel_profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"], "calls": v["calls"]}
+                           for k, v in prof.items()},
         "roofline": roof,
         "clocks": clk.summary(),
         "e2e": e2e,

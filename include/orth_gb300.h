@@ -197,8 +197,22 @@ void orth_gb300_last_status(orth_gb300_status *status);
  */
 void orth_gb300_last_host_timing(double out[4]);
 
-/* Number of device-wide reductions ("synchronizations") a call performs. */
+/*
+ * Number of device-wide reductions ("synchronizations") a call performs, from
+ * the variant's structure: each replaces one MPI_Allreduce of the reference
+ * (SRC/orth.c:113,132 then :187 or :196 per step for bcgsi2P1s; :277,286 then
+ * :332 or :341 for bcgsi21s; :423,437 per step for bcgspipi2; :514,526 for
+ * bcgsi2; :607,619 then :663 or :672 for bcgsi2P2s).
+ */
 int orth_gb300_sync_count(int variant, int n, int s);
+
+/*
+ * Number of device-wide reductions the last run on this thread actually
+ * launched: the fixed-order reduction kernel that replaces each MPI_Allreduce,
+ * counted at its launch site. Equals orth_gb300_sync_count for a run that
+ * completed.
+ */
+long long orth_gb300_last_reduction_count(void);
 
 /* Number of kernel launches the last run enqueued (for launch accounting). */
 long long orth_gb300_last_launch_count(void);
@@ -208,6 +222,8 @@ long long orth_gb300_last_launch_count(void);
  * records a CUDA event pair on the launching stream around every kernel group
  * of later runs; orth_gb300_profile_read waits for them and returns, per class, the
  * summed milliseconds, kernel launches, and algorithmic flops and bytes.
+ * Algorithmic bytes are FP64-equivalent in every precision: 8 bytes per element
+ * of each operand column the product reads once and each column it writes.
  * Classes: 0 tall Gram + reduction, 1 tall update, 2 small s x s kernels,
  * 3 TSQR, 4 digit slicing (split modes). Arrays have
  * orth_gb300_profile_classes() entries; any may be NULL. Returns 0 or a
@@ -216,6 +232,16 @@ long long orth_gb300_last_launch_count(void);
 void orth_gb300_profile(int on);
 int orth_gb300_profile_classes(void);
 int orth_gb300_profile_read(double *ms, long long *launches, double *flops, double *bytes);
+
+/*
+ * Per class, the bytes the kernels as built move at least, accumulated like
+ * orth_gb300_profile_read's (call it after that): equal to the algorithmic
+ * bytes for the FP64 form; for the split forms the operands' BF16 digit planes
+ * (2 bytes x digits per element) plus the FP64 columns written. calls[c]: the
+ * number of primitive calls (one Gram, one update, ...) timed in class c.
+ * Either array may be NULL. Returns 0.
+ */
+int orth_gb300_profile_traffic(double *bytes, long long *calls);
 
 /* Measure the FP64 pipe's throughput (TFLOP/s) with a DFMA loop; 0 or a cudaError_t. */
 int orth_gb300_fp64_peak_probe(double *tflops);

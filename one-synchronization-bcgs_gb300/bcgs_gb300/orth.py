@@ -64,6 +64,8 @@ def load(path: str | None = None):
     lib.orth_gb300_sync_count.restype = ctypes.c_int
     lib.orth_gb300_last_launch_count.argtypes = []
     lib.orth_gb300_last_launch_count.restype = ctypes.c_longlong
+    lib.orth_gb300_last_reduction_count.argtypes = []
+    lib.orth_gb300_last_reduction_count.restype = ctypes.c_longlong
     lib.orth_gb300_profile.argtypes = [ctypes.c_int]
     lib.orth_gb300_profile.restype = None
     lib.orth_gb300_profile_read.argtypes = [ctypes.POINTER(ctypes.c_double),
@@ -71,6 +73,8 @@ def load(path: str | None = None):
                                             ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_double)]
     lib.orth_gb300_profile_read.restype = ctypes.c_int
+    lib.orth_gb300_profile_traffic.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]
+    lib.orth_gb300_profile_traffic.restype = ctypes.c_int
     lib.orth_gb300_fp64_peak_probe.argtypes = [ctypes.POINTER(ctypes.c_double)]
     lib.orth_gb300_fp64_peak_probe.restype = ctypes.c_int
     lib.orth_gb300_bcgsi2P1s_dev_noalloc.argtypes = [
@@ -340,6 +344,11 @@ def last_launch_count() -> int:
     return int(load().orth_gb300_last_launch_count())
 
 
+def last_reduction_count() -> int:
+    """Device-wide reductions (synchronizations) the last run on this thread launched."""
+    return int(load().orth_gb300_last_reduction_count())
+
+
 PROFILE_CLASSES = ("gram", "update", "small", "tsqr", "slice")
 
 
@@ -349,7 +358,9 @@ def profile(on: bool) -> None:
 
 
 def profile_read() -> dict:
-    """Per class: ms, launches, algorithmic flops and bytes since profile(True)."""
+    """Per class since profile(True): ms, launches, algorithmic flops and bytes
+    (FP64-equivalent), and the bytes the kernels as built move (digit planes for
+    the split forms)."""
     k = len(PROFILE_CLASSES)
     ms = (ctypes.c_double * k)()
     ln = (ctypes.c_longlong * k)()
@@ -358,7 +369,11 @@ def profile_read() -> dict:
     rc = load().orth_gb300_profile_read(ms, ln, fl, by)
     if rc != 0:
         raise RuntimeError(f"orth_gb300_profile_read failed: {rc}")
-    return {c: {"ms": ms[i], "launches": ln[i], "flops": fl[i], "bytes": by[i]}
+    tr = (ctypes.c_double * k)()
+    calls = (ctypes.c_longlong * k)()
+    load().orth_gb300_profile_traffic(tr, calls)
+    return {c: {"ms": ms[i], "launches": ln[i], "flops": fl[i], "bytes": by[i], "traffic": tr[i],
+                "calls": calls[i]}
             for i, c in enumerate(PROFILE_CLASSES)}
 
 

@@ -6,6 +6,8 @@
 // gigabyte chunks, so a memset on the compute stream could wait behind them. A
 // kernel runs on the SMs and keeps the compute stream off the copy engines.
 #include <cstdint>
+#include <mutex>
+#include <vector>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -45,6 +47,32 @@ int zero_async(void* p, size_t bytes, cudaStream_t st) {
     ++g_launch_count;
     ++g_aux_launch_count;
     return (int)cudaGetLastError();
+}
+
+namespace {
+struct SmemAttr { int dev; const void* fn; int bytes; };
+std::vector<SmemAttr> g_smem_attrs;
+std::mutex g_smem_mu;
+}  // namespace
+
+// cudaFuncAttributeMaxDynamicSharedMemorySize is a per-device setting: a
+// process-wide "set once" would leave every GPU but the first at the 48 KB
+// default. This records what was set for each (device, kernel).
+int smem_attr(const void* fn, int bytes) {
+    int dev = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess) return (int)ce;
+    std::lock_guard<std::mutex> lock(g_smem_mu);
+    for (SmemAttr& a : g_smem_attrs) {
+        if (a.dev != dev || a.fn != fn) continue;
+        if (a.bytes >= bytes) return 0;
+        ce = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (ce == cudaSuccess) a.bytes = bytes;
+        return (int)ce;
+    }
+    ce = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (ce == cudaSuccess) g_smem_attrs.push_back({dev, fn, bytes});
+    return (int)ce;
 }
 
 }  // namespace bcgs

@@ -14,12 +14,19 @@ using i64 = long long;
 // Number of kernels enqueued by the launchers below since load (host counter;
 // split-precision batches enqueue from several host threads).
 extern std::atomic<long long> g_launch_count;
+// Number of launches of the fixed-order Gram reduction (the kernel that stands
+// in for each MPI_Allreduce of the reference).
+extern std::atomic<long long> g_reduce_count;
 
 // bytes of zeros at p, by a kernel on st (not a copy-engine memset). Counted in
 // g_launch_count and also in g_aux_launch_count, which the per-class profile
 // subtracts so that its launch counts are those of the classes' own kernels.
 int zero_async(void* p, size_t bytes, cudaStream_t st);
 extern std::atomic<long long> g_aux_launch_count;
+
+// Raises kernel fn's dynamic shared-memory limit to `bytes` on the current
+// device, once per (device, kernel). Call outside any stream capture.
+int smem_attr(const void* fn, int bytes);
 
 // C (na x nb, ld ldo) = X[:, a0:a0+na]^T X[:, b0:b0+nb] over m rows, FP64, with a
 // fixed-order two-stage reduction through `part` (nchunks * na * nb doubles).

@@ -20,9 +20,10 @@
 //     left in it. Calls whose work overlaps on the GPU (two streams, or two host
 //     threads) race on it; issue them one after another.
 //   * The first call on a device looks up the device address of the array
-//     (cudaGetSymbolAddress, with that device current) and also sets the
-//     shared-memory attributes of the kernels it launches. Make that first call
-//     before any stream capture.
+//     (cudaGetSymbolAddress, with that device current), and the launchers raise
+//     the shared-memory limits of the kernels it launches on that device (they
+//     record this per device and per kernel). Make that first call on each
+//     device before any stream capture.
 #include <cstdio>
 #include <mutex>
 
@@ -134,9 +135,10 @@ extern "C" int orth_gb300_bcgsi2P1s_dev_noalloc(int m, int n, int s, double* dX,
     double* tws = base + L.tsqr;
     const i64 M = m, ld = ldX;
 
-    // The status words must start at zero; everything else is written before it
-    // is read.
-    int err = (int)cudaMemsetAsync(stat, 0, kStatusWords * sizeof(int), st);
+    // The status words must start at zero (the array keeps the last call's
+    // contents); everything else is written before it is read. A kernel clears
+    // them, so the clear does not queue behind copy-engine work on the stream.
+    int err = zero_async(stat, kStatusWords * sizeof(int), st);
     auto gram = [&](int na, int b0, int nb, double* C) {
         if (err) return;
         err = launch_gram_fp64(dX, ld, M, 0, na, b0, nb, C, na, part,

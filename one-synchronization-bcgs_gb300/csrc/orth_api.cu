@@ -23,6 +23,7 @@
 namespace bcgs {
 
 std::atomic<long long> g_launch_count{0};
+std::atomic<long long> g_reduce_count{0};
 
 static inline bool is_split(int precision) {
     return precision == ORTH_GB300_SPLIT_BF16 || precision == ORTH_GB300_SPLIT_BF16_FAST;
@@ -85,9 +86,12 @@ std::mutex g_mu;
 // Optional per-kernel-class timing with CUDA events recorded on the launching
 // stream around each launch group. Classes: 0 tall Gram (incl. its reduction),
 // 1 tall update, 2 small s x s kernels, 3 TSQR, 4 digit slicing (split modes).
-// Algorithmic flops are FP64-equivalent (2 per multiply-add of the FP64 product);
-// algorithmic bytes are what the kernels must move: FP64 operands for the FP64
-// form, BF16 digit planes (2 bytes x digits per element) for the split forms.
+// Algorithmic flops are FP64-equivalent (2 per multiply-add of the FP64 product).
+// Algorithmic bytes are FP64-equivalent too: 8 bytes per element of every
+// operand column the product must read once and every column it writes, in any
+// precision. Traffic bytes are what the kernels as built move at least: the
+// same for the FP64 form; BF16 digit planes (2 bytes x digits per element) for
+// the operands the split forms read.
 constexpr int kProfClasses = 5;
 struct ProfPending { int cls; cudaEvent_t a, b; };
 struct Prof {
@@ -98,6 +102,8 @@ struct Prof {
     long long launches[kProfClasses] = {0, 0, 0, 0, 0};
     double flops[kProfClasses] = {0, 0, 0, 0, 0};
     double bytes[kProfClasses] = {0, 0, 0, 0, 0};
+    double traffic[kProfClasses] = {0, 0, 0, 0, 0};
+    long long calls[kProfClasses] = {0, 0, 0, 0, 0};
     cudaEvent_t get() {
         if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
         cudaEvent_t e = nullptr;
@@ -112,13 +118,15 @@ struct ProfScope {
     cudaStream_t st;
     cudaEvent_t a = nullptr;
     long long l0;
-    ProfScope(int c, cudaStream_t s, double flops, double bytes)
+    ProfScope(int c, cudaStream_t s, double flops, double bytes, double traffic = -1.0)
         : cls(c), st(s), l0(g_launch_count - g_aux_launch_count) {
         if (!g_prof.on) return;
         a = g_prof.get();
         cudaEventRecord(a, st);
         g_prof.flops[cls] += flops;
         g_prof.bytes[cls] += bytes;
+        g_prof.traffic[cls] += traffic < 0.0 ? bytes : traffic;
+        g_prof.calls[cls] += 1;
     }
     ~ProfScope() {
         if (!g_prof.on) return;
@@ -147,6 +155,7 @@ int host_precision() {
     return g_host_precision;
 }
 std::atomic<long long> g_last_launches{0};
+thread_local long long g_last_reductions = 0;
 
 int init_ctx() {
     if (g_ctx.init) return 0;
@@ -333,7 +342,7 @@ struct Engine {
             if (err) return;
         }
         const double eb = is_split(precision) ? 2.0 * split_digits() : 8.0;
-        ProfScope ps(0, st, 2.0 * m * na * nb, eb * m * (na + nb));
+        ProfScope ps(0, st, 2.0 * m * na * nb, 8.0 * m * (na + nb), eb * m * (na + nb));
         if (is_split(precision)) {
             err = launch_gram_split(X, ld, m, na, b0, nb, C, na, scr().split.as<char>(),
                                     scr().split.bytes, g_ctx.num_sms, st);
@@ -351,9 +360,9 @@ struct Engine {
             err = split_prepare(K + nc, st);
             if (err) return;
         }
-        const double bytes = is_split(precision) ? 2.0 * split_digits() * m * (K + nc) + 8.0 * m * nc
-                                                 : 8.0 * m * (K + 2.0 * nc);
-        ProfScope ps(1, st, 2.0 * m * K * nc + (T ? (double)m * nc * nc : 0.0), bytes);
+        const double traffic = is_split(precision) ? 2.0 * split_digits() * m * (K + nc) + 8.0 * m * nc
+                                                   : 8.0 * m * (K + 2.0 * nc);
+        ProfScope ps(1, st, 2.0 * m * K * nc + (T ? (double)m * nc * nc : 0.0), 8.0 * m * (K + 2.0 * nc), traffic);
         if (is_split(precision)) {
             err = launch_update_split(X, ld, m, K, c0, nc, S, lds, T, ldt, scr().split.as<char>(),
                                       scr().split.bytes, g_ctx.num_sms, st);
@@ -371,8 +380,9 @@ struct Engine {
             err = split_prepare(K + s + nz, st);
             if (err) return;
         }
-        const double bytes = 2.0 * split_digits() * m * (K + s + nz) + 8.0 * m * (s + nz);
-        ProfScope ps(1, st, 2.0 * m * K * (s + nz) + (double)m * (s * s + nz * nz), bytes);
+        const double traffic = 2.0 * split_digits() * m * (K + s + nz) + 8.0 * m * (s + nz);
+        ProfScope ps(1, st, 2.0 * m * K * (s + nz) + (double)m * (s * s + nz * nz),
+                     8.0 * m * (K + s + nz) + 8.0 * m * (s + nz), traffic);
         err = launch_fused_update_split(X, ld, m, K, s, nz, G, ldg, Ty, Sp, K + s, Ts, g_ctx.num_sms, st);
     }
     void pyth_chol(const double* Om, int ldom, const double* A, int lda, int k, int nz, double* T,
@@ -673,6 +683,7 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
         return 3;
     }
     const long long launches0 = g_launch_count;
+    const long long reductions0 = g_reduce_count;
     Engine e{dX, (i64)ldX, (i64)m, n, s, dR, ldR, precision, st,
              carve_small(scr().small.as<double>(), n, s), scr().status.as<int>()};
     e.link = link;
@@ -692,6 +703,7 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
         default: run_p2s(e); break;
     }
     g_last_launches = g_launch_count - launches0;
+    g_last_reductions = g_reduce_count - reductions0;
     if (link && !e.err) {
         link->finish(st);
         if (link->err) e.err = link->err;
@@ -1099,12 +1111,15 @@ int orth_gb300_sync_count(int variant, int n, int s) {
 
 long long orth_gb300_last_launch_count(void) { return g_last_launches; }
 
+long long orth_gb300_last_reduction_count(void) { return g_last_reductions; }
+
 void orth_gb300_profile(int on) {
     std::lock_guard<std::mutex> lock(g_mu);
     for (auto& p : g_prof.pending) { g_prof.pool.push_back(p.a); g_prof.pool.push_back(p.b); }
     g_prof.pending.clear();
     for (int c = 0; c < kProfClasses; ++c) {
-        g_prof.ms[c] = 0; g_prof.launches[c] = 0; g_prof.flops[c] = 0; g_prof.bytes[c] = 0;
+        g_prof.ms[c] = 0; g_prof.launches[c] = 0; g_prof.flops[c] = 0; g_prof.bytes[c] = 0; g_prof.traffic[c] = 0;
+        g_prof.calls[c] = 0;
     }
     g_prof.on = on != 0;
 }
@@ -1128,6 +1143,15 @@ int orth_gb300_profile_read(double* ms, long long* launches, double* flops, doub
         if (launches) launches[c] = g_prof.launches[c];
         if (flops) flops[c] = g_prof.flops[c];
         if (bytes) bytes[c] = g_prof.bytes[c];
+    }
+    return 0;
+}
+
+int orth_gb300_profile_traffic(double* bytes, long long* calls) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    for (int c = 0; c < kProfClasses; ++c) {
+        if (bytes) bytes[c] = g_prof.traffic[c];
+        if (calls) calls[c] = g_prof.calls[c];
     }
     return 0;
 }

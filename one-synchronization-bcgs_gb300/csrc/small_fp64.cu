@@ -212,9 +212,8 @@ int launch_scol(const double* G, int ldg, int mZ, int s, int nZ, const double* Y
     if (nZ <= 0) return 0;
     if (s > SMAX || nZ > SMAX) return (int)cudaErrorInvalidValue;
     const size_t smem = (size_t)SMAX * (nZ + s) * sizeof(double);
-    static const cudaError_t attr_rc = cudaFuncSetAttribute(   // once, thread-safe
-        scol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(SMAX * 2 * SMAX * sizeof(double)));
-    if (attr_rc != cudaSuccess) return (int)attr_rc;
+    const int attr_rc = smem_attr((const void*)scol_kernel, (int)(SMAX * 2 * SMAX * sizeof(double)));
+    if (attr_rc) return attr_rc;
     scol_kernel<<<1, SM_THREADS, smem, st>>>(G, ldg, mZ, s, nZ, Yd, ldy, Scol, ldsc);
     g_launch_count += 1;
     return (int)cudaGetLastError();

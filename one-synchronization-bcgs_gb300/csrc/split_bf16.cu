@@ -32,8 +32,9 @@
 // owner, warps 2-9: epilogue, two threads per TMEM lane), with an A-tile ring of
 // 16 KB slots, a B ring, and two TMEM accumulators so the epilogue of one window
 // overlaps the MMAs of the next. The update is persistent and takes row tiles from
-// a per-launch counter; the Gram's M-block CTAs of one row range form a cluster that
-// shares each B tile by TMA multicast. Every wait is bounded; a timeout sets an
+// a per-launch counter; the Gram's M-block CTAs of one row range run side by side
+// and share each B tile through L2 (B loaded evict_last, A evict_first). No load
+// is multicast. Every wait is bounded; a timeout sets an
 // error word and the kernel winds down.
 #include <cstdio>
 #include <cstring>
@@ -461,47 +462,29 @@ __device__ __forceinline__ double assemble(long long hi, long long mid, float lo
     return __longlong_as_double((long long)(sign | ((unsigned long long)E << 52) | (mant & 0xFFFFFFFFFFFFFULL)));
 }
 
-// Producer: for each chunk, B planes then KD A planes (TMA).
+// Producer: for each chunk, B planes then KD A planes (TMA), each with its L2
+// eviction policy (polA, polB).
 template <int NB, int KD, class CoordFn>
 __device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapA, const CUtensorMap* mapB, uint8_t* sA,
                                               uint8_t* sB, Bars* bars, Ring& ra, Ring& rb, CoordFn coords,
-                                              int item, int ch, volatile int* abort, int* err, int cs = 1,
-                                              int rank = 0) {
+                                              int item, int ch, volatile int* abort, int* err, uint64_t polA,
+                                              uint64_t polB) {
     constexpr int B_SLOT = SmemLayout<NB, KD>::B_SLOT;
     // Plane p of A is at (ax, ay, az + p*azs); plane p of B at (bx, by, bz + p*bzs).
     int ax, ay, az, azs, bx, by, bz, bzs;
     coords(item, ch, ax, ay, az, azs, bx, by, bz, bzs);
-    if (cs == 1) {
-        if (!tc::mbar_wait(&bars->b_empty[rb.slot], rb.phase ^ 1u, abort, err, 11)) return false;
-        tc::mbar_expect_tx(&bars->b_full[rb.slot], (uint32_t)B_SLOT);
+    if (!tc::mbar_wait(&bars->b_empty[rb.slot], rb.phase ^ 1u, abort, err, 11)) return false;
+    tc::mbar_expect_tx(&bars->b_full[rb.slot], (uint32_t)B_SLOT);
 #pragma unroll
-        for (int j = 0; j < KD; ++j)
-            tc::tma_load_3d(sB + rb.slot * B_SLOT + j * NB * KCH * 2, mapB, &bars->b_full[rb.slot], bx, by,
-                            bz + j * bzs);
-    } else if (rank == 0) {
-        // Cluster leader: the B slot is free in every CTA once all cs MMA threads
-        // released it (remote arrivals on this CTA's b_empty); one multicast load
-        // fills it everywhere.
-        if (!tc::mbar_wait(&bars->b_empty[rb.slot], rb.phase ^ 1u, abort, err, 13)) return false;
-        tc::mbar_expect_tx(&bars->b_full[rb.slot], (uint32_t)B_SLOT);
-        const uint16_t mask = (uint16_t)((1u << cs) - 1u);
-#pragma unroll
-        for (int j = 0; j < KD; ++j)
-            tc::tma_load_3d_mc(sB + rb.slot * B_SLOT + j * NB * KCH * 2, mapB, &bars->b_full[rb.slot], bx, by,
-                               bz + j * bzs, mask);
-    } else {
-        // Other CTAs only arm their own b_full for the bytes the leader sends, once
-        // the previous use of the slot has completed here (no second arrival may
-        // fall into a phase that is still open).
-        if (!tc::mbar_wait(&bars->b_full[rb.slot], rb.phase ^ 1u, abort, err, 14)) return false;
-        tc::mbar_expect_tx(&bars->b_full[rb.slot], (uint32_t)B_SLOT);
-    }
+    for (int j = 0; j < KD; ++j)
+        tc::tma_load_3d_hint(sB + rb.slot * B_SLOT + j * NB * KCH * 2, mapB, &bars->b_full[rb.slot], bx, by,
+                             bz + j * bzs, polB);
     rb.advance(RB);
 #pragma unroll
     for (int i = 0; i < KD; ++i) {
         if (!tc::mbar_wait(&bars->a_empty[ra.slot], ra.phase ^ 1u, abort, err, 12 + 100 * ra.slot)) return false;
         tc::mbar_expect_tx(&bars->a_full[ra.slot], (uint32_t)A_SLOT);
-        tc::tma_load_3d(sA + ra.slot * A_SLOT, mapA, &bars->a_full[ra.slot], ax, ay, az + i * azs);
+        tc::tma_load_3d_hint(sA + ra.slot * A_SLOT, mapA, &bars->a_full[ra.slot], ax, ay, az + i * azs, polA);
         ra.advance(RA);
     }
     return true;
@@ -512,7 +495,7 @@ __device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapA, const CUt
 template <int NB, int KD, bool A_MN = false>
 __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uint8_t* sA, uint8_t* sB,
                                           Bars* bars, Ring& ra, Ring& rb, bool first_in_window,
-                                          volatile int* abort, int* err, int cs = 1) {
+                                          volatile int* abort, int* err) {
     constexpr int B_SLOT = SmemLayout<NB, KD>::B_SLOT;
     if (!tc::mbar_wait(&bars->b_full[rb.slot], rb.phase, abort, err, 21)) return false;
     const uint32_t b_addr = tc::smem_u32(sB + rb.slot * B_SLOT);
@@ -534,15 +517,13 @@ __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uin
         tc::mma_commit(&bars->a_empty[ra.slot]);
         ra.advance(RA);
     }
-    if (cs == 1) tc::mma_commit(&bars->b_empty[rb.slot]);
-    else tc::mma_commit_mc(&bars->b_empty[rb.slot], (uint16_t)1u);   // release to the cluster leader
+    tc::mma_commit(&bars->b_empty[rb.slot]);
     rb.advance(RB);
     return true;
 }
 
 template <int NB, int KD>
-__device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint8_t*& sB, uint32_t* tmem_slot,
-                                           int cs = 1) {
+__device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint8_t*& sB, uint32_t* tmem_slot) {
     using L = SmemLayout<NB, KD>;
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     sA = base + L::A_OFF;
@@ -551,8 +532,7 @@ __device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint
     const int warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         for (int i = 0; i < RA; ++i) { tc::mbar_init(&bars->a_full[i], 1); tc::mbar_init(&bars->a_empty[i], 1); }
-        // b_empty counts one release per CTA of the cluster (cs = 1: no cluster).
-        for (int i = 0; i < RB; ++i) { tc::mbar_init(&bars->b_full[i], 1); tc::mbar_init(&bars->b_empty[i], (uint32_t)cs); }
+        for (int i = 0; i < RB; ++i) { tc::mbar_init(&bars->b_full[i], 1); tc::mbar_init(&bars->b_empty[i], 1); }
         for (int i = 0; i < 2; ++i) { tc::mbar_init(&bars->t_full[i], 1); tc::mbar_init(&bars->t_empty[i], NEPI); }
         tc::mbar_init(&bars->drain, 1);
         // Tile-number ring: one producer; the MMA thread and the 8 epilogue warps read.
@@ -572,7 +552,7 @@ __device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint
 // ---------------------------------------------------------------------------
 struct GramParams {
     int na, nb, b0, nrc;
-    int cs;          // cluster size: the numMB CTAs of one (row range, N-group) share B by multicast
+    int a_once;      // 1: every A tile is read by one CTA only (numNG == 1), loaded evict_first
     i64 m;
     int numMB, numNG, rc;
     i64 rows_per;   // multiple of WIN*KCH
@@ -591,10 +571,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     __shared__ volatile int abort_flag;
     uint8_t *sA, *sB;
     if (threadIdx.x == 0) abort_flag = 0;
-    const int cs = p.cs;
-    Bars* bars = setup_cta<NB, KD>(smem_raw, sA, sB, &tmem_slot, cs);
-    const int rank = cs > 1 ? (int)tc::cluster_rank() : 0;
-    if (cs > 1) tc::cluster_sync();   // peers' barriers are initialized before any remote arrive
+    Bars* bars = setup_cta<NB, KD>(smem_raw, sA, sB, &tmem_slot);
     const uint32_t tmem = tmem_slot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -615,10 +592,14 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
 
     if (warp == 0) {
         if (lane == 0) {
+            // The numMB CTAs of one (row range, N-group) read the same B tiles at
+            // about the same time: B stays in L2 (evict_last) for the others.
+            const uint64_t polA = p.a_once ? tc::policy_evict_first() : tc::policy_evict_normal();
+            const uint64_t polB = tc::policy_evict_last();
             Ring ra, rb;
             for (int ch = 0; ch < nchunks; ++ch)
-                if (!produce_chunk<NB, KD>(&mapA, &mapB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag, p.err, cs,
-                                           rank))
+                if (!produce_chunk<NB, KD>(&mapA, &mapB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag, p.err,
+                                           polA, polB))
                     break;
             if (abort_flag) {
                 drain_ring(bars->a_full, RA, ra);
@@ -637,7 +618,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
                 const int c_end = min(nchunks, (w + 1) * WIN);
                 for (int ch = w * WIN; ch < c_end && ok; ++ch)
                     ok = mma_chunk<NB, KD>(tmem, (uint32_t)(buf * L::TMEM_COLS_PER_BUF), sA, sB, bars, ra, rb,
-                                       ch == w * WIN, &abort_flag, p.err, cs);
+                                       ch == w * WIN, &abort_flag, p.err);
                 if (ok) tc::mma_commit(&bars->t_full[buf]);
             }
             tc::mma_commit(&bars->drain);
@@ -679,15 +660,9 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     }
     __syncthreads();
     if (warp == 1) {
-        // All MMAs issued by this CTA have completed once `drain` fires (then its
-        // last remote releases have reached the leader too).
+        // All MMAs issued by this CTA have completed once `drain` fires.
         if (lane == 0) tc::mbar_wait(&bars->drain, 0, &abort_flag, p.err, 51);
         __syncwarp();
-    }
-    // No CTA leaves while a peer may still arrive on its barriers or receive its
-    // multicast; every CTA reaches this point, also after a wait gave up.
-    if (cs > 1) tc::cluster_sync();
-    if (warp == 1) {
         tc::tc_fence_after();
         tc::tmem_dealloc(tmem, (uint32_t)L::TMEM_ALLOC);
     }
@@ -743,6 +718,9 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     __shared__ int s_tile[RQ];
     if (warp == 0) {
         if (lane == 0) {
+            // A tiles are read once per launch; the right-hand factor by every CTA.
+            const uint64_t polA = tc::policy_evict_first();
+            const uint64_t polB = tc::policy_evict_last();
             Ring ra, rb, rq;
             bool ok = true;
             while (ok) {
@@ -753,7 +731,8 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
                 rq.advance(RQ);
                 if (tile >= ntiles) break;
                 for (int ch = 0; ch < nchunks && ok; ++ch)
-                    ok = produce_chunk<NB, KD>(&mapA, &mapB, sA, sB, bars, ra, rb, coords, tile, ch, &abort_flag, p.err);
+                    ok = produce_chunk<NB, KD>(&mapA, &mapB, sA, sB, bars, ra, rb, coords, tile, ch, &abort_flag, p.err,
+                                               polA, polB);
             }
             if (abort_flag) {
                 drain_ring(bars->a_full, RA, ra);
@@ -990,7 +969,7 @@ int ensure_fresh(int c_begin, int c_end, cudaStream_t st) {
 
 template <class K>
 int set_smem(K kernel, int bytes) {
-    return (int)cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return smem_attr((const void*)kernel, bytes);
 }
 
 }  // namespace
@@ -1036,16 +1015,14 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     if (!rc) rc = make_map3(&P.map_bdig16, P.bdig, P.kpad, 16, KD_MAX, P.kpad, 16 * P.kpad, 16);
     if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
     if (rc) return rc;
-    static const int attrs_rc = [] {   // once, thread-safe
-        int r = set_smem(gram_tc_kernel<6>, SmemLayout<32, 6>::BYTES);
-        if (!r) r = set_smem(gram_tc_kernel<7>, SmemLayout<32, 7>::BYTES);
-        if (!r) r = set_smem(update_tc_kernel<16, 6>, SmemLayout<16, 6>::BYTES);
-        if (!r) r = set_smem(update_tc_kernel<16, 7>, SmemLayout<16, 7>::BYTES);
-        if (!r) r = set_smem(update_tc_kernel<32, 6>, SmemLayout<32, 6>::BYTES);
-        if (!r) r = set_smem(update_tc_kernel<32, 7>, SmemLayout<32, 7>::BYTES);
-        return r;
-    }();
-    return attrs_rc;
+    // Shared-memory limits of the tensor-core kernels on this device.
+    rc = set_smem(gram_tc_kernel<6>, SmemLayout<32, 6>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<7>, SmemLayout<32, 7>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<16, 6>, SmemLayout<16, 6>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<16, 7>, SmemLayout<16, 7>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<32, 6>, SmemLayout<32, 6>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<32, 7>, SmemLayout<32, 7>::BYTES);
+    return rc;
 }
 
 void split_mark_stale(int c0, int nc) {
@@ -1104,52 +1081,14 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     gp.part = P.part;
     gp.err = P.err;
     if ((i64)gp.rc * na * nb > P.part_doubles) return (int)cudaErrorInvalidValue;
-    // The numMB CTAs of one (row range, N-group) are consecutive in blockIdx.x; as a
-    // cluster they read each B tile once (multicast) instead of numMB times.
-    gp.cs = (gp.numMB > 1 && gp.numMB <= 8) ? gp.numMB : 1;
-    cudaLaunchConfig_t cfg = {};
-    if (gp.cs > 1) {
-        // Clusters must sit whole inside a GPC: take only as many row ranges as can
-        // run at once, so that the launch is a single wave of clusters.
-        cudaLaunchConfig_t q = {};
-        cudaLaunchAttribute qa[1];
-        q.gridDim = dim3((unsigned)(mbn * gp.rc));
-        q.blockDim = dim3(NTHREADS);
-        q.dynamicSmemBytes = P.kd == 6 ? SmemLayout<32, 6>::BYTES : SmemLayout<32, 7>::BYTES;
-        qa[0].id = cudaLaunchAttributeClusterDimension;
-        qa[0].val.clusterDim.x = (unsigned)gp.cs;
-        qa[0].val.clusterDim.y = 1;
-        qa[0].val.clusterDim.z = 1;
-        q.attrs = qa;
-        q.numAttrs = 1;
-        int maxc = 0;
-        cudaError_t oe = P.kd == 6 ? cudaOccupancyMaxActiveClusters(&maxc, gram_tc_kernel<6>, &q)
-                                   : cudaOccupancyMaxActiveClusters(&maxc, gram_tc_kernel<7>, &q);
-        if (oe == cudaSuccess && maxc > 0) {
-            const int rc_fit = maxc / gp.numNG > 0 ? maxc / gp.numNG : 1;
-            if (rc_fit < gp.rc) {
-                gp.rows_per = round_up(ceil_div(m, rc_fit), (i64)WIN * KCH);
-                gp.rc = (int)ceil_div(m, gp.rows_per);
-            }
-        } else {
-            (void)cudaGetLastError();
-            gp.cs = 1;
-        }
-    }
-    cudaLaunchAttribute attr[1];
-    cfg.gridDim = dim3((unsigned)(mbn * gp.rc));
-    cfg.blockDim = dim3(NTHREADS);
-    cfg.dynamicSmemBytes = P.kd == 6 ? SmemLayout<32, 6>::BYTES : SmemLayout<32, 7>::BYTES;
-    cfg.stream = st;
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = (unsigned)gp.cs;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaError_t lce = P.kd == 6 ? cudaLaunchKernelEx(&cfg, gram_tc_kernel<6>, P.map_col_a, P.map_col_b, gp)
-                                : cudaLaunchKernelEx(&cfg, gram_tc_kernel<7>, P.map_col_a, P.map_col_b, gp);
-    if (lce != cudaSuccess) return (int)lce;
+    // One wave of CTAs: numMB x numNG per row range. The numMB CTAs of one
+    // (row range, N-group) are consecutive in blockIdx.x, so they run at the
+    // same time and share each B tile through L2.
+    gp.a_once = gp.numNG == 1 ? 1 : 0;
+    const unsigned grid = (unsigned)(mbn * gp.rc);
+    const int smem = P.kd == 6 ? SmemLayout<32, 6>::BYTES : SmemLayout<32, 7>::BYTES;
+    if (P.kd == 6) gram_tc_kernel<6><<<grid, NTHREADS, smem, st>>>(P.map_col_a, P.map_col_b, gp);
+    else gram_tc_kernel<7><<<grid, NTHREADS, smem, st>>>(P.map_col_a, P.map_col_b, gp);
     g_launch_count += 1;
     rc = (int)cudaGetLastError();
     if (rc) return rc;
@@ -1226,9 +1165,8 @@ int launch_fused_update_split(double* X, i64 ld, i64 m, int K, int s, int nz, co
     if (rc) return rc;
     cudaError_t ce = (cudaError_t)zero_async(P.bmax, 128 * sizeof(unsigned long long), st);
     if (ce != cudaSuccess) return (int)ce;
-    static const cudaError_t fattr_rc = cudaFuncSetAttribute(   // once, thread-safe
-        bbuild_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(3 * 64 * 65 * sizeof(double)));
-    if (fattr_rc != cudaSuccess) return (int)fattr_rc;
+    const int fattr_rc = set_smem(bbuild_fused_kernel, (int)(3 * 64 * 65 * sizeof(double)));
+    if (fattr_rc) return fattr_rc;
     bbuild_fused_kernel<<<(unsigned)ceil_div(kin, 64), 256, 3 * 64 * 65 * sizeof(double), st>>>(G, ldg, K, s, Ty, s, Sp, ldsp, Ts, nz, nz,
                                                                         P.cexp, P.bfull, (int)P.kpad, P.bmax);
     g_launch_count += 1;

@@ -162,6 +162,7 @@ int launch_gram_fp64(const double* X, i64 ld, i64 m, int a0, int na, int b0, int
     if (blocks > 4 * 152) blocks = 4 * 152;
     gram_reduce<<<blocks, 256, 0, st>>>(part, nchunks, na, nb, out, ldo);
     g_launch_count += 2;
+    g_reduce_count += 1;
     return (int)cudaGetLastError();
 }
 
@@ -172,6 +173,7 @@ int launch_gram_reduce(const double* part, int nchunks, int na, int nb, double* 
     if (blocks > 4 * 152) blocks = 4 * 152;
     gram_reduce<<<blocks, 256, 0, st>>>(part, nchunks, na, nb, out, ldo);
     g_launch_count += 1;
+    g_reduce_count += 1;
     return (int)cudaGetLastError();
 }
 

@@ -300,9 +300,8 @@ static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR
                     cudaStream_t st) {
     const int TR = tsqr_tile_rows(nc);
     const size_t smem = tsqr_tile_smem_bytes(TR, NC);
-    static const cudaError_t attr_rc = cudaFuncSetAttribute(   // once, thread-safe
-        tsqr_tile_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (attr_rc != cudaSuccess) return (int)attr_rc;
+    const int attr_rc = smem_attr((const void*)tsqr_tile_kernel<NC>, (int)smem);
+    if (attr_rc) return attr_rc;
     // Level matrices: level 0 is the panel itself; level l >= 1 lives in ws.
     constexpr int kMaxLevels = 48;   // each level divides the rows by TR / nc >= 2: 2^k rows need at most k levels
     double* lvl_ptr[kMaxLevels];

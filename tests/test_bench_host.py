@@ -53,3 +53,22 @@ def test_algorithmic_counts_at_config1():
     assert abs(bench.alg_bytes_p1s(m, n, s) - 6.70e11) / 6.70e11 < 0.01
     assert bench.alg_flops_p1s(m, n, s) == 4.0 * m * n * n + 8.0 * m * n * s
     assert abs(bench.alg_flops_p1s(m, n, s) - 9.35e12) / 9.35e12 < 0.01
+
+
+def test_reference_arm_runs_full_size_steps_within_budget():
+    """--impl reference times whole QRs of the configured size (no scaling), runs
+    no more steps than asked or than the budget allows, and says how many ran."""
+    import json
+    import subprocess
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--m", "8192",
+                        "--n", "64", "--s", "16", "--steps", "3", "--warmup", "2", "--ref-budget-s", "60"],
+                       capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "ms"
+    assert 1 <= line["steps"] <= 3 and line["steps_requested"] == 3 and line["warmup"] == 1
+    assert len(line["step_ms"]) == line["steps"]
+    assert abs(sum(line["step_ms"]) / line["steps"] - line["value"]) < 0.2
+    assert "m=8192" in line["config"]["workload"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"

@@ -101,3 +101,24 @@ def test_port_matches_reference_at_config0():
         sign = np.sign(np.diag(R)) * np.sign(np.diag(Rref))
         assert np.max(np.abs(sign[:, None] * R - Rref)) <= qr_tolerance(kappa) * np.max(np.abs(Rref))
         assert port.loo_2(Q) <= 10 * max(float(g[f"{v}/loo_2"]), 1e-15)
+
+
+@pytest.mark.parametrize("variant", ["bcgsi2P1s", "bcgsi21s"])
+def test_port_matches_kappa_sweep_fixture(variant):
+    """The restated oracle against the reference's own results at kappa = 1e10 on
+    the reduced config-1 construction (tests/golden/kappa_sweep.npz): the same
+    breakdown step (P1s breaks down there), and where there is none, the same
+    metrics."""
+    import os
+    from bcgs_gb300 import inputs
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "kappa_sweep.npz"))
+    case = "graded_k1e10"
+    m, n, s, seed = (int(z[f"{case}/{k}"]) for k in ("m", "n", "s", "seed"))
+    X = inputs.graded_host(m, n, float(z[f"{case}/kappa"]), seed=seed)
+    Q, R, info = port.run_variant(variant, X, n, s)
+    assert info == int(z[f"{case}/{variant}/info"])
+    if info:
+        return
+    _, loo2, res = z[f"{case}/{variant}/metrics"]
+    assert abs(port.loo_2(Q) - loo2) <= 0.5 * loo2
+    assert abs(port.rel_residual(X, Q, R) - res) <= 0.5 * res

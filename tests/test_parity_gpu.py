@@ -26,13 +26,20 @@ def _compare(X, Q, R, Qref, Rref, cond):
     assert np.max(np.abs(Qs - Qr)) <= tol
 
 
+@pytest.mark.parametrize("precision", ["fp64", "split7"])
 @pytest.mark.parametrize("case", sorted(GOLD))
 @pytest.mark.parametrize("variant", VARIANTS)
-def test_golden_fp64(lib, case, variant):
+def test_golden(lib, case, variant, precision):
+    """The reference's own outputs (tests/golden/bcgs_golden.npz) through the orth.h
+    host entry points, in FP64 and in the 56-bit split form."""
     g = GOLD[case]
     X, n, s = g["X"], g["n"], g["s"]
     gv = g[variant]
-    Q, R, rc, st = orth.qr(variant, X, s)
+    assert orth.set_host_precision(orth.FP64 if precision == "fp64" else orth.SPLIT_BF16) == 0
+    try:
+        Q, R, rc, st = orth.qr(variant, X, s)
+    finally:
+        orth.set_host_precision(orth.FP64)
     assert rc == 0 and st["cuda_error"] == 0
     if gv["info"] != 0:
         if case == "edge_n2s_plus4" and variant == "bcgsi2P1s":
@@ -203,3 +210,28 @@ def test_large_properties_fp64(lib):
         res = float(((E * E).sum() / (X0 * X0).sum()).sqrt().item())
         assert loo < 1e-12, (variant, loo)
         assert res < 1e-14, (variant, res)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split7"])
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_measured_sync_count(lib, variant, precision):
+    """The number of device-wide reductions a run launches (counted where the
+    reduction kernel is launched) equals the variant's structure: p + 1 for the
+    one-sync variants (one per block step after the first step's two), 2p for
+    bcgspipi2 and bcgsi2. Reference: the MPI_Allreduce calls at SRC/orth.c:113,132,
+    187/196 (P1s); :277,286,332/341 (21s); :423,437 (PIPI); :514,526 (BCGS2);
+    :607,619,663/672 (P2s)."""
+    torch = pytest.importorskip("torch")
+    m, n, s = 20000, 96, 16
+    X = inputs.graded_host(m, n, 1e4, seed=8)
+    prec = orth.FP64 if precision == "fp64" else orth.SPLIT_BF16
+    dX = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
+    dR = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    rc, st = orth.run_dev(variant, m, n, s, dX.data_ptr(), m, dR.data_ptr(), n, prec,
+                          torch.cuda.current_stream().cuda_stream)
+    assert rc == 0 and st["breakdown_step"] == 0
+    p = (n - s) // s
+    expected = {"bcgsi2P1s": p + 1, "bcgsi21s": p + 1, "bcgsi2P2s": p + 1,
+                "bcgspipi2": 2 * p, "bcgsi2": 2 * p}[variant]
+    assert orth.sync_count(variant, n, s) == expected
+    assert orth.last_reduction_count() == expected
