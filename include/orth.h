@@ -11,13 +11,16 @@
  *   bcgsi2     BCGSI+ (BCGS2) with TSQR intra-orthogonalization  (SRC/orth.c:464-548)
  *   bcgsi2P2s  BCGSI+P-2S, TSQR first pass + one synchronization (SRC/orth.c:550-697)
  *
- * Arguments (all host memory, column-major FP64, as in the reference):
+ * Arguments (column-major FP64, as in the reference; host memory as in the
+ * reference, or device/managed memory, detected with cudaPointerGetAttributes):
  *   m       rows of X. With one GPU there is one rank, so Xsub holds all m rows.
  *   n, s    columns of X and the block width; n >= 2s, 1 <= s <= 64. The last
  *           block may be ragged (n - s not a multiple of s).
- *   Xsub    m x n, leading dimension ldXsub >= m; overwritten with Q.
+ *   Xsub    m x n, leading dimension ldXsub >= m; overwritten with Q. In host
+ *           memory it is streamed to the GPU and back in column chunks while
+ *           the QR runs; in device memory the QR runs on it in place.
  *   R       n x n, leading dimension ldR >= n; the upper block triangle is
- *           written, the rest is left untouched.
+ *           written, the rest is left untouched (host or device memory).
  *   work    not accessed (the GPU keeps its own workspace); lwork is checked
  *           with the reference's rule: >= 5ns + 9s^2 + m*n (m*s for bcgsi2),
  *           evaluated in 64 bits and capped at INT_MAX.
@@ -26,7 +29,8 @@
  * reference prints); 2 invalid arguments; 3 CUDA failure. A Cholesky breakdown
  * of a Pythagorean-shifted Gram block does not change the return code (the
  * reference ignores dpotrf's info too); it is reported by
- * orth_gb300_last_status() in orth_gb300.h.
+ * orth_gb300_last_status() in orth_gb300.h. Every call returns after its
+ * results are in Xsub and R, as the reference's does.
  */
 #ifndef ORTH_H
 #define ORTH_H

@@ -74,6 +74,26 @@ int orth_gb300_bcgsi2P1s_dev_noalloc(int m, int n, int s, double *dX, long long 
 int orth_gb300_set_host_precision(int precision);
 
 /*
+ * IntraOrtho of the panels the reference factors with Trilinos TSQR (block 1 of
+ * every variant, SRC/orth.c:105-107 and its counterparts; each step's panels in
+ * bcgsi2, :520-523 and :532-535, and in bcgsi2P2s, :612-614 and :649-652):
+ *   ORTH_GB300_INTRA_TSQR     the hand-written TSQR tree (default, the reference's choice)
+ *   ORTH_GB300_INTRA_CHOLQR2  CholeskyQR2: twice G = V^T V (one deterministic
+ *                             reduction each), T = chol(G), V = V T^{-1}; R = R2 R1.
+ *                             Cheaper (two tall passes), but its Cholesky breaks down
+ *                             for panels with condition number beyond about 1e8;
+ *                             a breakdown is reported like a Pythagorean one (status
+ *                             breakdown_step = the block step).
+ * Applies to the orth.h entry points and orth_gb300_run_dev, in every precision
+ * (the panel factorization runs in FP64); batched plans and the allocation-free
+ * entry point always use TSQR. The environment variable ORTH_GB300_INTRA = tsqr |
+ * cholqr2 sets it at first use. Returns 0, or 2 for an unknown mode.
+ */
+#define ORTH_GB300_INTRA_TSQR 0
+#define ORTH_GB300_INTRA_CHOLQR2 1
+int orth_gb300_set_intra_ortho(int mode);
+
+/*
  * Diagnostic of the split-precision kernels: the last nonzero error word, i.e. the
  * code of a bounded wait that ran out (for the operand-ring waits, code + 100 *
  * ring slot), or 0 if none has.

@@ -81,6 +81,8 @@ def load(path: str | None = None):
         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong,
         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(Status)]
     lib.orth_gb300_bcgsi2P1s_dev_noalloc.restype = ctypes.c_int
+    lib.orth_gb300_set_intra_ortho.argtypes = [ctypes.c_int]
+    lib.orth_gb300_set_intra_ortho.restype = ctypes.c_int
     lib.orth_gb300_set_host_precision.argtypes = [ctypes.c_int]
     lib.orth_gb300_set_host_precision.restype = ctypes.c_int
     lib.orth_gb300_last_split_error.argtypes = []
@@ -153,6 +155,19 @@ def call(variant: str, m: int, n: int, s: int, Xsub: np.ndarray, ldXsub: int, R:
     return int(getattr(lib, variant)(m, n, s, _dp(Xsub), ldXsub, _dp(R), ldR, _dp(work), lwork))
 
 
+def call_ptr(variant: str, m: int, n: int, s: int, x_ptr: int, ldXsub: int, r_ptr: int, ldR: int,
+             lwork: int | None = None) -> int:
+    """Call the orth.h entry point ``variant`` with raw addresses (host or device
+    memory, e.g. ``tensor.data_ptr()``), as C code holding such pointers would."""
+    lib = load()
+    if lwork is None:
+        lwork = lwork_min(m, n, s, variant)
+    dp = ctypes.POINTER(ctypes.c_double)
+    work = np.zeros(1)
+    return int(getattr(lib, variant)(m, n, s, ctypes.cast(ctypes.c_void_p(x_ptr), dp), ldXsub,
+                                     ctypes.cast(ctypes.c_void_p(r_ptr), dp), ldR, _dp(work), lwork))
+
+
 def qr(variant: str, X0: np.ndarray, s: int):
     """Convenience: QR of a copy of X0 (m x n) through the orth.h entry point.
 
@@ -215,6 +230,16 @@ def bcgsi2P1s_dev_noalloc(m: int, n: int, s: int, x_ptr: int, ldx: int, r_ptr: i
 def set_host_precision(precision: int) -> int:
     """Precision of the orth.h entry points (FP64, SPLIT_BF16, SPLIT_BF16_FAST)."""
     return int(load().orth_gb300_set_host_precision(precision))
+
+
+INTRA_TSQR = 0
+INTRA_CHOLQR2 = 1
+
+
+def set_intra_ortho(mode: int) -> int:
+    """IntraOrtho of the panels the reference factors with TSQR: INTRA_TSQR
+    (default) or INTRA_CHOLQR2."""
+    return int(load().orth_gb300_set_intra_ortho(mode))
 
 
 def last_split_error() -> int:

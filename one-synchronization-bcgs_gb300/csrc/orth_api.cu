@@ -154,6 +154,19 @@ int host_precision() {
     }
     return g_host_precision;
 }
+// IntraOrtho of the panels the reference hands to TSQR (block 1 of every
+// variant; each step's panels in bcgsi2 and bcgsi2P2s): the TSQR tree (the
+// reference's choice, default) or CholQR2, set through orth_gb300_set_intra_ortho
+// or ORTH_GB300_INTRA ("tsqr", "cholqr2") at first use.
+int g_intra_mode = -1;
+int intra_mode() {
+    if (g_intra_mode < 0) {
+        g_intra_mode = ORTH_GB300_INTRA_TSQR;
+        const char* e = getenv("ORTH_GB300_INTRA");
+        if (e && strcmp(e, "cholqr2") == 0) g_intra_mode = ORTH_GB300_INTRA_CHOLQR2;
+    }
+    return g_intra_mode;
+}
 std::atomic<long long> g_last_launches{0};
 thread_local long long g_last_reductions = 0;
 
@@ -191,10 +204,11 @@ struct Small {
     double* S0;    // s x s first-step coefficients
     double* Sd;    // s x s
     double* Yd;    // s x s
+    double* Cq;    // 3 s x s: CholQR2's panel Gram, R1 and R2
 };
 
 i64 small_doubles(int n, int s) {
-    return 2LL * (n + s) * 2 * s + (i64)n * s + 3LL * s * s + 64;
+    return 2LL * (n + s) * 2 * s + (i64)n * s + 6LL * s * s + 64;
 }
 
 Small carve_small(double* base, int n, int s) {
@@ -205,6 +219,7 @@ Small carve_small(double* base, int n, int s) {
     w.S0 = w.Scol + (i64)n * s;
     w.Sd = w.S0 + (i64)s * s;
     w.Yd = w.Sd + (i64)s * s;
+    w.Cq = w.Yd + (i64)s * s;
     return w;
 }
 
@@ -410,6 +425,31 @@ struct Engine {
         err = launch_tsqr(X, ld, m, c0, nc, Rout, ldr, scr().tsqr.as<double>(), st);
         if (is_split(precision)) split_mark_stale(c0, nc);
     }
+    // CholQR2 of X[:, c0:c0+nc] (FP64 in every precision): twice G = V^T V (one
+    // deterministic reduction), T = chol(G), V = V T^{-1}; then R = R2 R1 into
+    // (Rout, ldr). A Cholesky breakdown is recorded as block step `step`.
+    void cholqr2(int c0, int nc, double* Rout, int ldr, int step) {
+        if (err) return;
+        host_sync(c0 + nc, c0);
+        ProfScope ps(3, st, 2.0 * (2.0 * m * nc * nc + (double)m * nc * nc), 8.0 * m * nc * 6.0);
+        double* G = w.Cq;
+        double* R1 = G + (i64)s * s;
+        double* R2 = R1 + (i64)s * s;
+        for (int pass = 0; pass < 2 && !err; ++pass) {
+            double* T = pass ? R2 : R1;
+            err = launch_gram_fp64(X, ld, m, c0, nc, c0, nc, G, nc, scr().part.as<double>(),
+                                   gram_chunks_fp64(m, nc, nc, g_ctx.num_sms), st);
+            if (!err) err = launch_pyth_chol(G, nc, nullptr, 0, 0, nc, T, nc, status, step, st);
+            if (!err) err = launch_update_fp64(X, ld, m, 0, 0, c0, nc, nullptr, 0, T, nc, st);
+        }
+        if (!err) err = launch_rblock(Rout, ldr, 0, 0, nc, nullptr, 0, nullptr, 0, R1, nc, R2, nc, 0, st);
+        if (is_split(precision)) split_mark_stale(c0, nc);
+    }
+    // IntraOrtho of the panel X[:, c0:c0+nc] (where the reference calls TSQR).
+    void intra(int c0, int nc, double* Rout, int ldr, int step) {
+        if (intra_mode() == ORTH_GB300_INTRA_CHOLQR2) cholqr2(c0, nc, Rout, ldr, step);
+        else tsqr(c0, nc, Rout, ldr);
+    }
 };
 
 int nblocks_after_first(int n, int s) { return (n - s + s - 1) / s; }  // p = ceil((n-s0)/s)
@@ -420,7 +460,7 @@ void run_p1s(Engine& e) {
     const int s = e.s, n = e.n, s0 = s;
     const int p = nblocks_after_first(n, s);
     Small& w = e.w;
-    e.tsqr(0, s0, e.R, e.ldR);                                       // :105-107
+    e.intra(0, s0, e.R, e.ldR, 1);                                   // :105-107
     // First step (:110-147).
     double* W = w.G2;                                                // 2s x s, ld 2s
     e.gram(2 * s, s0, s, W);                                         // :111-114
@@ -473,7 +513,7 @@ void run_lagged_fused(Engine& e, bool pyth) {
     const int p = nblocks_after_first(n, s);
     Small& w = e.w;
     const int mode = pyth ? 0 : 1;
-    e.tsqr(0, s0, e.R, e.ldR);
+    e.intra(0, s0, e.R, e.ldR, 1);
     double* W = w.G2;
     int nZ = n - s - s0 < s ? n - s - s0 : s;
     int na, nb;
@@ -542,7 +582,7 @@ void run_21s(Engine& e) {
     const int s = e.s, n = e.n, s0 = s;
     const int p = nblocks_after_first(n, s);
     Small& w = e.w;
-    e.tsqr(0, s0, e.R, e.ldR);                                       // :269-271
+    e.intra(0, s0, e.R, e.ldR, 1);                                   // :269-271
     e.gram(s0, s0, s, w.S0);                                         // :275-278
     e.update(s0, s0, s, w.S0, s0, nullptr, 0);                       // :280-281
     int nZ = n - s - s0 < s ? n - s - s0 : s;                        // :282
@@ -585,7 +625,7 @@ void run_pipi(Engine& e) {
     const int s = e.s, n = e.n, s0 = s;
     const int p = nblocks_after_first(n, s);
     Small& w = e.w;
-    e.tsqr(0, s0, e.R, e.ldR);                                       // :411-413
+    e.intra(0, s0, e.R, e.ldR, 1);                                   // :411-413
     int mScol = s0;
     for (int i = 0; i < p; ++i) {
         const int nZ = n - i * s - s0 < s ? n - i * s - s0 : s;       // :419
@@ -607,16 +647,16 @@ void run_bcgsi2(Engine& e) {
     const int s = e.s, n = e.n, s0 = s;
     const int p = nblocks_after_first(n, s);
     Small& w = e.w;
-    e.tsqr(0, s0, e.R, e.ldR);                                       // :503-505
+    e.intra(0, s0, e.R, e.ldR, 1);                                   // :503-505
     int mScol = s0;
     for (int i = 0; i < p; ++i) {
         const int nZ = n - i * s - s0 < s ? n - i * s - s0 : s;       // :511
         e.gram(mScol, mScol, nZ, w.G1);                              // :512-515
         e.update(mScol, mScol, nZ, w.G1, mScol, nullptr, 0);         // :518-519
-        e.tsqr(mScol, nZ, w.Sd, nZ);                                 // :520-523
+        e.intra(mScol, nZ, w.Sd, nZ, i + 1);                         // :520-523
         e.gram(mScol, mScol, nZ, w.G2);                              // :524-527
         e.update(mScol, mScol, nZ, w.G2, mScol, nullptr, 0);         // :530-531
-        e.tsqr(mScol, nZ, w.Yd, nZ);                                 // :532-535
+        e.intra(mScol, nZ, w.Yd, nZ, i + 1);                         // :532-535
         e.rblock(mScol, mScol, nZ, w.G1, mScol, w.G2, mScol, w.Sd, w.Yd, 0);  // :537-541
         mScol += s;
     }
@@ -628,10 +668,10 @@ void run_p2s(Engine& e) {
     const int s = e.s, n = e.n, s0 = s;
     const int p = nblocks_after_first(n, s);
     Small& w = e.w;
-    e.tsqr(0, s0, e.R, e.ldR);                                       // :599-601
+    e.intra(0, s0, e.R, e.ldR, 1);                                   // :599-601
     e.gram(s0, s0, s, w.S0);                                         // :605-608
     e.update(s0, s0, s, w.S0, s0, nullptr, 0);                       // :610-611
-    e.tsqr(s0, s, w.Sd, s);                                          // :612-614
+    e.intra(s0, s, w.Sd, s, 1);                                      // :612-614
     int nZ = n - s - s0 < s ? n - s - s0 : s;                        // :615
     int na = 2 * s, nb = s + nZ;
     double* G = w.G1;
@@ -644,7 +684,7 @@ void run_p2s(Engine& e) {
         const int mScol = mZ + s;
         e.scol(G, ldg, mZ, nZ, w.Yd, w.Scol);                        // :641-645
         e.update(mScol, mScol, nZ, w.Scol, mScol, nullptr, 0);       // :647-648
-        e.tsqr(mScol, nZ, w.Sd, nZ);                                 // :649-652
+        e.intra(mScol, nZ, w.Sd, nZ, i + 1);                         // :649-652
         int nY, nZn;
         if (i < p - 1) {                                             // :653-666
             nZn = n - (i + 1) * s - s0 < s ? n - (i + 1) * s - s0 : s;
@@ -730,6 +770,61 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
     return e.err ? 3 : 0;
 }
 
+// Whether p is memory the GPU can address directly (device or managed memory).
+bool is_device_pointer(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Copies what the reference writes into R (SRC/orth.c): for column j of block b,
+// rows [0, end of block b); bcgsi21s writes only the upper triangle of its
+// diagonal blocks after the first (SRC/orth.c:302,360 use dlacpy 'U').
+cudaError_t write_back_r(int variant, int n, int s, const double* src, int lds, double* dst, int ldd,
+                         cudaMemcpyKind kind) {
+    for (int j = 0; j < n; ++j) {
+        const int b = j / s;
+        int rows = (b + 1) * s < n ? (b + 1) * s : n;
+        if (variant == ORTH_GB300_BCGSI21S && b >= 1) rows = j + 1;
+        cudaError_t ce = cudaMemcpy(dst + (size_t)j * ldd, src + (size_t)j * lds, (size_t)rows * sizeof(double), kind);
+        if (ce != cudaSuccess) return ce;
+    }
+    return cudaSuccess;
+}
+
+// orth.h entry point called with X in device (or managed) memory: the QR runs in
+// place on the caller's buffer, with no staging. R is written in place when it is
+// device memory too (the kernels write exactly the reference's part of R), else
+// through a device copy and the write-back rule. Synchronous, like the reference.
+int run_on_device_buffers(int variant, int m, int n, int s, double* dX, int ldX, double* R, int ldR, bool r_dev,
+                          int precision) {
+    cudaStream_t st = g_ctx.stream;
+    orth_gb300_status stt;
+    std::memset(&stt, 0, sizeof(stt));
+    double* dR = R;
+    int ldr = ldR;
+    if (!r_dev) {
+        if (g_ctx.hostR.ensure((size_t)n * n * sizeof(double))) return 3;
+        dR = g_ctx.hostR.as<double>();
+        ldr = n;
+        if (zero_async(dR, (size_t)n * n * sizeof(double), st)) return 3;
+    }
+    int rc = run_device(variant, m, n, s, dX, ldX, dR, ldr, precision, st, &stt);
+    if (!rc && !r_dev) {
+        cudaError_t ce = cudaStreamSynchronize(st);
+        if (ce == cudaSuccess) ce = write_back_r(variant, n, s, dR, n, R, ldR, cudaMemcpyDeviceToHost);
+        if (ce != cudaSuccess) {
+            stt.cuda_error = (int)ce;
+            rc = 3;
+        }
+    }
+    g_last_status = stt;
+    return rc;
+}
+
 // Host-buffer form (the orth.h ABI).
 int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double* R, int ldR,
              double* work, int lwork, int precision) {
@@ -749,6 +844,8 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
     int rc = init_ctx();
     if (rc) return 3;
     cudaStream_t st = g_ctx.stream;
+    const bool x_dev = is_device_pointer(Xsub), r_dev = is_device_pointer(R);
+    if (x_dev) return run_on_device_buffers(variant, m, n, s, Xsub, ldXsub, R, ldR, r_dev, precision);
     const size_t xbytes = (size_t)m * n * sizeof(double);
     const size_t rbytes = (size_t)n * n * sizeof(double);
     if (g_ctx.hostX.ensure(xbytes) || g_ctx.hostR.ensure(rbytes)) return 3;
@@ -819,6 +916,16 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
     // [0, end of block b); bcgsi21s writes only the upper triangle of its
     // diagonal blocks after the first (SRC/orth.c:302,360 use dlacpy 'U').
     const double* hs = g_ctx.hostR_stage;
+    if (r_dev) {
+        ce = write_back_r(variant, n, s, hs, n, R, ldR, cudaMemcpyHostToDevice);
+        if (ce != cudaSuccess) {
+            stt.cuda_error = (int)ce;
+            g_last_status = stt;
+            return 3;
+        }
+        g_last_status = stt;
+        return 0;
+    }
     for (int j = 0; j < n; ++j) {
         const int b = j / s;
         int rows = (b + 1) * s < n ? (b + 1) * s : n;
@@ -985,6 +1092,13 @@ int orth_gb300_set_host_precision(int precision) {
 }
 
 int orth_gb300_last_split_error(void) { return split_last_error(); }
+
+int orth_gb300_set_intra_ortho(int mode) {
+    if (mode != ORTH_GB300_INTRA_TSQR && mode != ORTH_GB300_INTRA_CHOLQR2) return 2;
+    std::lock_guard<std::mutex> lock(g_mu);
+    g_intra_mode = mode;
+    return 0;
+}
 
 int orth_gb300_split_supported(int m, int n, int s) { return split_supported(m, n, s) ? 1 : 0; }
 

@@ -37,7 +37,7 @@ import scipy.linalg.lapack as _lapack
 
 __all__ = [
     "bcgsi2P1s", "bcgsi21s", "bcgspipi2", "bcgsi2", "bcgsi2P2s", "VARIANTS",
-    "tsqr_explicit", "loo_fro", "loo_2", "residual_fro", "rel_residual",
+    "tsqr_explicit", "cholqr2_explicit", "loo_fro", "loo_2", "residual_fro", "rel_residual",
     "run_variant",
 ]
 
@@ -104,6 +104,61 @@ def tsqr_explicit(A: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     return np.asfortranarray(q[:, :n]), np.asfortranarray(R)
 
 
+def cholqr2_explicit(A: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """CholeskyQR2 of a tall panel: twice G = V^T V (dgemm 'T','N'),
+    T = chol(G) (dpotrf 'U'), V = V T^{-1} (dtrsm 'R','U','N','N'); R = T2 T1.
+
+    Not in the reference, which factors every panel with TSQR; this restates the
+    published algorithm (Fukaya, Nakatsukasa, Yanagisawa, Yamamoto, "CholeskyQR2",
+    2014) for the library's CholQR2 IntraOrtho option. A Cholesky breakdown
+    carries on with the partial factor, as the reference does with dpotrf.
+    """
+    V = np.array(A, order="F", copy=True)
+    Ts = []
+    for _ in range(2):
+        T, _info = _chol_upper(_gram(V, V))
+        _trsm_right_upper(V, T)
+        Ts.append(T)
+    return V, np.asfortranarray(np.triu(Ts[1] @ Ts[0]))
+
+
+def tsqr_tree_explicit(A: np.ndarray, TR: int = 256) -> tuple[np.ndarray, np.ndarray]:
+    """Explicit thin QR by a TSQR reduction tree: Householder QR (LAPACK) of each
+    TR-row tile, then of the stack of the tiles' R factors the same way, until one
+    tile remains; the root's diag(R) made >= 0; Q by the down-sweep. The shape of
+    the library's GPU TSQR, restated to show how a panel's Q depends on the tree
+    when the panel is numerically rank deficient (for full-rank panels every
+    explicit QR agrees up to column signs)."""
+    m, n = A.shape
+    if m <= TR:
+        Q, R = np.linalg.qr(A)
+        d = np.sign(np.diag(R))
+        d[d == 0] = 1
+        return np.asfortranarray(Q * d), np.asfortranarray(R * d[:, None])
+    Qs, Rs = [], []
+    for r0 in range(0, m, TR):
+        t = A[r0:r0 + TR]
+        h = t.shape[0]
+        if h < n:
+            t = np.vstack([t, np.zeros((n - h, n))])
+        q, r = np.linalg.qr(t)
+        Qs.append(q[:h])
+        Rs.append(r)
+    Qr, R = tsqr_tree_explicit(np.vstack(Rs), TR)
+    Q = np.vstack([Qs[i] @ Qr[i * n:(i + 1) * n] for i in range(len(Qs))])
+    return np.asfortranarray(Q), np.asfortranarray(R)
+
+
+_INTRA = {"tsqr": tsqr_explicit, "cholqr2": cholqr2_explicit, "tsqr_tree": tsqr_tree_explicit}
+_intra_fn = [tsqr_explicit]
+
+
+def _intra_qr(A: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """The IntraOrtho in force for this run (TSQR, as in the reference, unless
+    run_variant was asked for CholQR2)."""
+    return _intra_fn[0](A)
+
+
 def _nblocks(n: int, s: int) -> int:
     """p = ceil((n - s0)/s) with s0 = s (SRC/orth.c:55)."""
     return int(math.ceil((n - s) / float(s)))
@@ -125,7 +180,7 @@ def _first_block(X: np.ndarray, s: int, R: np.ndarray) -> None:
 
     SRC/orth.c:105-107 (same in every variant).
     """
-    Q1, R11 = tsqr_explicit(X[:, :s])
+    Q1, R11 = _intra_qr(X[:, :s])
     X[:, :s] = Q1
     R[:s, :s] = R11
 
@@ -312,11 +367,11 @@ def bcgsi2(X: np.ndarray, n: int, s: int, R: np.ndarray) -> int:
         Xk = X[:, mScol:mScol + nZ]
         S = _gram(X[:, :mScol], Xk)                          # :512-515
         _sub_prod(Xk, X[:, :mScol], S)                       # :518-519
-        Qk, Sdiag = tsqr_explicit(Xk)                        # :520-523
+        Qk, Sdiag = _intra_qr(Xk)                        # :520-523
         Xk[...] = Qk
         Y = _gram(X[:, :mScol], Xk)                          # :524-527
         _sub_prod(Xk, X[:, :mScol], Y)                       # :530-531
-        Qk, Ydiag = tsqr_explicit(Xk)                        # :532-535
+        Qk, Ydiag = _intra_qr(Xk)                        # :532-535
         Xk[...] = Qk
         R[:mScol, mScol:mScol + nZ] = S + Y @ Sdiag          # :537-539
         R[mScol:mScol + nZ, mScol:mScol + nZ] = Ydiag @ Sdiag  # :540-541
@@ -338,7 +393,7 @@ def bcgsi2P2s(X: np.ndarray, n: int, s: int, R: np.ndarray) -> int:
     S12 = _gram(X[:, :s0], X[:, s0:s0 + s])                  # :605-608
     R[:s0, s0:s0 + s] = S12                                  # :609
     _sub_prod(X[:, s0:s0 + s], X[:, :s0], S12)               # :610-611
-    Qk, Sdiag = tsqr_explicit(X[:, s0:s0 + s])               # :612-614
+    Qk, Sdiag = _intra_qr(X[:, s0:s0 + s])               # :612-614
     X[:, s0:s0 + s] = Qk
     nZ = min(s, n - s - s0)                                  # :615
     s2 = s + nZ
@@ -358,7 +413,7 @@ def bcgsi2P2s(X: np.ndarray, n: int, s: int, R: np.ndarray) -> int:
         _trsm_left_upper_trans(Ydiag, Scol[mZ:mScol, :])     # :644-645
         Xk = X[:, mScol:mScol + nZ]
         _sub_prod(Xk, X[:, :mScol], Scol)                    # :647-648
-        Qk, Sdiag = tsqr_explicit(Xk)                        # :649-652
+        Qk, Sdiag = _intra_qr(Xk)                        # :649-652
         Xk[...] = Qk
         if i < p - 1:                                        # :653-666
             nZn = min(s, n - (i + 1) * s - s0)
@@ -392,13 +447,20 @@ VARIANTS = {
 }
 
 
-def run_variant(name: str, X0: np.ndarray, n: int, s: int):
-    """Run one variant on a copy of X0 (m x n). Returns (Q, R, info)."""
+def run_variant(name: str, X0: np.ndarray, n: int, s: int, intra: str = "tsqr"):
+    """Run one variant on a copy of X0 (m x n). Returns (Q, R, info).
+
+    intra: "tsqr" (the reference's IntraOrtho, restated as LAPACK Householder QR),
+    "tsqr_tree" (a TSQR reduction tree) or "cholqr2"."""
     m = X0.shape[0]
     X = np.zeros((m, max(n + s, 3 * s)), order="F")
     X[:, :n] = X0[:, :n]
     R = np.zeros((n, n), order="F")
-    info = VARIANTS[name](X, n, s, R)
+    _intra_fn[0] = _INTRA[intra]
+    try:
+        info = VARIANTS[name](X, n, s, R)
+    finally:
+        _intra_fn[0] = tsqr_explicit
     return np.array(X[:, :n], order="F"), R, info
 
 

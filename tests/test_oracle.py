@@ -122,3 +122,48 @@ def test_port_matches_kappa_sweep_fixture(variant):
     _, loo2, res = z[f"{case}/{variant}/metrics"]
     assert abs(port.loo_2(Q) - loo2) <= 0.5 * loo2
     assert abs(port.rel_residual(X, Q, R) - res) <= 0.5 * res
+
+
+def test_cholqr2_restatement_is_a_qr():
+    """The oracle's CholQR2 (the library's alternative IntraOrtho) gives the same
+    factorization as its TSQR on a moderately conditioned panel."""
+    from bcgs_gb300 import inputs
+    A = inputs.graded_host(5000, 16, 1e4, seed=3)
+    Qc, Rc = port.cholqr2_explicit(A)
+    Qt, Rt = port.tsqr_explicit(A)
+    assert np.all(np.diag(Rc) > 0)
+    Qc, Rc = sign_normalize(Qc, Rc)
+    Qt, Rt = sign_normalize(Qt, Rt)
+    assert np.max(np.abs(Qc - Qt)) <= qr_tolerance(1e4)
+    assert np.max(np.abs(Rc - Rt)) <= qr_tolerance(1e4) * np.max(np.abs(Rt))
+    assert port.loo_2(Qc) < 1e-14
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_port_cholqr2_variants(variant):
+    from bcgs_gb300 import inputs
+    X = inputs.graded_host(3000, 48, 1e5, seed=4)
+    Q, R, info = port.run_variant(variant, X, 48, 8, intra="cholqr2")
+    assert info == 0
+    assert port.loo_2(Q) < 1e-13 and port.rel_residual(X, Q, R) < 1e-14
+
+
+def test_p2s_breakdown_on_rank_deficient_panels_depends_on_the_tsqr():
+    """On the s-step monomial basis the panels bcgsi2P2s hands to TSQR are
+    numerically rank deficient; an explicit QR of such a panel is unique only up
+    to its rounding noise, so the step at which the following Pythagorean pass
+    breaks down depends on the TSQR implementation: the same restated algorithm
+    breaks down at very different steps with LAPACK Householder QR (the stand-in
+    for the reference's Trilinos TSQR) and with a 256-row TSQR tree (the GPU
+    TSQR's shape). The GPU parity test therefore does not pin this step."""
+    from bcgs_gb300 import inputs
+    X = inputs.monomial_host(16384, 128, 8, seed=4321)
+    _, _, step_lapack = port.run_variant("bcgsi2P2s", X, 128, 8)
+    _, _, step_tree = port.run_variant("bcgsi2P2s", X, 128, 8, intra="tsqr_tree")
+    assert step_lapack > 0 and step_tree > 0
+    assert abs(step_lapack - step_tree) > 1, (step_lapack, step_tree)
+    # For a full-rank panel both explicit QRs agree up to column signs.
+    A = inputs.graded_host(4096, 16, 1e3, seed=1)
+    Q1, R1 = sign_normalize(*port.tsqr_explicit(A))
+    Q2, R2 = sign_normalize(*port.tsqr_tree_explicit(A))
+    assert np.max(np.abs(Q1 - Q2)) <= qr_tolerance(1e3)

@@ -235,3 +235,37 @@ def test_measured_sync_count(lib, variant, precision):
                 "bcgspipi2": 2 * p, "bcgsi2": 2 * p}[variant]
     assert orth.sync_count(variant, n, s) == expected
     assert orth.last_reduction_count() == expected
+
+
+@pytest.mark.parametrize("variant", ["bcgsi2P1s", "bcgsi21s", "bcgsi2"])
+@pytest.mark.parametrize("r_on_device", [True, False])
+def test_orth_h_with_device_pointers(lib, variant, r_on_device):
+    """The orth.h entry points given device buffers (detected with
+    cudaPointerGetAttributes): the QR runs in place on them, bit-identical to
+    the host-buffer call; R gets exactly the reference's part (the rest keeps
+    its sentinel), in device or host memory."""
+    torch = pytest.importorskip("torch")
+    m, n, s, ldx = 30000, 64, 16, 30011
+    X = inputs.graded_host(m, n, 1e5, seed=13)
+    Qh, Rh, rc, _ = orth.qr(variant, X, s)
+    assert rc == 0
+    dX = torch.full((n, ldx), 7.0, dtype=torch.float64, device="cuda")
+    dX[:, :m] = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
+    if r_on_device:
+        Rbuf = torch.full((n, n), -3.0, dtype=torch.float64, device="cuda")
+        r_ptr = Rbuf.data_ptr()
+    else:
+        Rnp = np.full((n, n), -3.0, order="F")
+        r_ptr = Rnp.ctypes.data
+    torch.cuda.synchronize()
+    rc = orth.call_ptr(variant, m, n, s, dX.data_ptr(), ldx, r_ptr, n)
+    assert rc == 0
+    Q = dX[:, :m].cpu().numpy().T
+    R = Rbuf.cpu().numpy().T if r_on_device else Rnp
+    assert np.array_equal(Q, Qh)
+    assert bool((dX[:, m:] == 7.0).all())
+    for j in range(n):
+        b = j // s
+        rows = min((b + 1) * s, n) if not (variant == "bcgsi21s" and b >= 1) else j + 1
+        assert np.array_equal(R[:rows, j], Rh[:rows, j]), j
+        assert np.all(R[(b + 1) * s:, j] == -3.0), j
