@@ -74,6 +74,45 @@ int orth_gb300_bcgsi2P1s_dev_noalloc(int m, int n, int s, double *dX, long long 
 int orth_gb300_set_host_precision(int precision);
 
 /*
+ * Row-sharded runs: one rank per GPU, each holding a contiguous block of rows
+ * of X, as the reference's MPI ranks do (SRC/orth.c:69-76 partitions m rows;
+ * every MPI_Allreduce sums the ranks' partial Gram blocks). The partition is the
+ * reference's rule applied to chunks of ORTH_GB300_SHARD_ROWS rows:
+ * orth_gb300_shard_rows gives this rank's first row and row count (host
+ * arithmetic, no GPU; 2 if some rank would get no chunk). Each rank then calls
+ * orth_gb300_run_sharded with its rows (dXsub: msub x n, ldX >= msub, device
+ * memory, overwritten with its rows of Q) and a full n x n dR (device memory,
+ * written on every rank). Only FP64 (the reference's arithmetic).
+ *
+ * Instead of an allreduce, each synchronization gathers every rank's per-chunk
+ * partial Gram sums and adds them in global chunk order on every rank, and the
+ * TSQR gathers its leaf tiles' R factors and runs the upper tree on every rank.
+ * So Q and R do not depend on the number of ranks: they are bit-identical to a
+ * one-rank call of orth_gb300_run_sharded on all of X.
+ *
+ * comm->allgather(ctx, send, recv, count, stream) must copy `count` doubles from
+ * `send` on every rank into recv[r * count ...] for r = 0 .. size-1 (device
+ * pointers on this rank's GPU), ordered after the work enqueued on `stream`
+ * before the call and before the work enqueued after it returns: e.g.
+ * ncclAllGather on that stream, or a stream synchronize plus a host-staged
+ * MPI_Allgather. It returns 0 on success. The callback is called from the
+ * calling thread only. Return codes as orth_gb300_run_dev, plus 2 for an
+ * invalid communicator or partition. Synchronizes the stream before returning.
+ */
+#define ORTH_GB300_SHARD_ROWS 8192
+typedef int (*orth_gb300_allgather_fn)(void *ctx, const double *send, double *recv, long long count,
+                                       void *stream);
+typedef struct orth_gb300_comm {
+    int rank, size;
+    orth_gb300_allgather_fn allgather;
+    void *ctx;
+} orth_gb300_comm;
+int orth_gb300_shard_rows(long long m, int size, int rank, long long *row0, long long *msub);
+int orth_gb300_run_sharded(int variant, long long m, int n, int s, double *dXsub, long long ldX,
+                           double *dR, int ldR, void *stream, const orth_gb300_comm *comm,
+                           orth_gb300_status *status);
+
+/*
  * IntraOrtho of the panels the reference factors with Trilinos TSQR (block 1 of
  * every variant, SRC/orth.c:105-107 and its counterparts; each step's panels in
  * bcgsi2, :520-523 and :532-535, and in bcgsi2P2s, :612-614 and :649-652):

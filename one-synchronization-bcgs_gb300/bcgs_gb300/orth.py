@@ -29,6 +29,16 @@ class Status(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+ALLGATHER_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                ctypes.c_longlong, ctypes.c_void_p)
+
+
+class Comm(ctypes.Structure):
+    """orth_gb300_comm: this rank, the rank count and the allgather callback."""
+    _fields_ = [("rank", ctypes.c_int), ("size", ctypes.c_int), ("allgather", ALLGATHER_FN),
+                ("ctx", ctypes.c_void_p)]
+
+
 _lib = None
 
 
@@ -81,6 +91,13 @@ def load(path: str | None = None):
         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong,
         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(Status)]
     lib.orth_gb300_bcgsi2P1s_dev_noalloc.restype = ctypes.c_int
+    lib.orth_gb300_shard_rows.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
+    lib.orth_gb300_shard_rows.restype = ctypes.c_int
+    lib.orth_gb300_run_sharded.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_void_p, ctypes.POINTER(Comm), ctypes.POINTER(Status)]
+    lib.orth_gb300_run_sharded.restype = ctypes.c_int
     lib.orth_gb300_set_intra_ortho.argtypes = [ctypes.c_int]
     lib.orth_gb300_set_intra_ortho.restype = ctypes.c_int
     lib.orth_gb300_set_host_precision.argtypes = [ctypes.c_int]
@@ -234,6 +251,85 @@ def set_host_precision(precision: int) -> int:
 
 INTRA_TSQR = 0
 INTRA_CHOLQR2 = 1
+
+
+SHARD_ROWS = 8192
+
+
+def shard_rows(m: int, size: int, rank: int):
+    """This rank's (first row, row count) in a row-sharded run of m rows
+    (orth_gb300_shard_rows; host arithmetic). Raises if a rank would get no rows."""
+    r0, ms = ctypes.c_longlong(0), ctypes.c_longlong(0)
+    rc = int(load().orth_gb300_shard_rows(m, size, rank, ctypes.byref(r0), ctypes.byref(ms)))
+    if rc != 0:
+        raise ValueError(f"no valid partition of {m} rows over {size} ranks")
+    return r0.value, ms.value
+
+
+def host_staged_allgather(gather_host):
+    """An orth_gb300_allgather_fn that stages through host memory: it waits for the
+    stream, copies `count` doubles of `send` to the host, calls
+    gather_host(numpy array) -> list of every rank's arrays in rank order (for
+    example torch.distributed.all_gather over gloo or MPI), and copies them back
+    into `recv`. Keep the returned object alive while it is in use."""
+    import torch
+
+    def cb(ctx, send, recv, count, stream):
+        try:
+            n = int(count)
+            st = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
+            st.synchronize()
+            host = np.empty(n, dtype=np.float64)
+            cudart = _cudart()
+            if cudart.cudaMemcpy(ctypes.c_void_p(host.ctypes.data), ctypes.c_void_p(send), n * 8, 2) != 0:
+                return 1
+            parts = gather_host(host)
+            allh = np.ascontiguousarray(np.concatenate(parts))
+            if cudart.cudaMemcpy(ctypes.c_void_p(recv), ctypes.c_void_p(allh.ctypes.data), allh.nbytes, 1) != 0:
+                return 1
+            return 0
+        except Exception:
+            return 1
+
+    return ALLGATHER_FN(cb)
+
+
+_cudart_lib = None
+
+
+def _cudart():
+    """The CUDA runtime this library links (for the host-staged exchange)."""
+    global _cudart_lib
+    if _cudart_lib is None:
+        import glob
+        import torch
+        cands = sorted(glob.glob(os.path.join(os.path.dirname(torch.__file__), "lib", "libcudart.so*")))
+        cands += sorted(glob.glob(os.path.join(os.path.dirname(os.path.dirname(torch.__file__)), "nvidia",
+                                               "cuda_runtime", "lib", "libcudart.so*")))
+        cands += ["libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"]
+        for c in cands:
+            try:
+                _cudart_lib = ctypes.CDLL(c)
+                break
+            except OSError:
+                continue
+        if _cudart_lib is None:
+            raise RuntimeError("libcudart not found")
+        _cudart_lib.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+        _cudart_lib.cudaMemcpy.restype = ctypes.c_int
+    return _cudart_lib
+
+
+def run_sharded(variant: str, m: int, n: int, s: int, x_ptr: int, ldx: int, r_ptr: int, ldr: int,
+                rank: int, size: int, allgather, stream: int = 0):
+    """One rank of a row-sharded run (orth_gb300_run_sharded): this rank's rows of
+    X at x_ptr (device), a full R at r_ptr (device). Returns (rc, status dict)."""
+    comm = Comm(rank, size, allgather, None)
+    st = Status()
+    rc = int(load().orth_gb300_run_sharded(VARIANT_ID[variant], m, n, s, ctypes.c_void_p(x_ptr), ldx,
+                                           ctypes.c_void_p(r_ptr), ldr, ctypes.c_void_p(stream),
+                                           ctypes.byref(comm), ctypes.byref(st)))
+    return rc, st.as_dict()
 
 
 def set_intra_ortho(mode: int) -> int:

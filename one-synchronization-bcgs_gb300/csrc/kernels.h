@@ -59,6 +59,33 @@ i64 tsqr_workspace_doubles(i64 m, int nc);
 int launch_tsqr(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR, double* ws,
                 cudaStream_t st);
 
+// Exchange of the row-sharded path: gathers `count` doubles from every rank into
+// `all` (size * count doubles, rank order), ordered on stream st. 0 on success.
+typedef int (*ShardGatherFn)(void* ctx, const double* mine, double* all, long long count, cudaStream_t st);
+
+// Row-sharded TSQR of this rank's rows X[0:m_local, c0:c0+nc] (TR-row tiles
+// [t0[rank], t0[rank] + nt[rank]) of T). `mine` holds maxt * nc * nc doubles and
+// `all` size times that; ws holds tsqr_workspace_doubles(T * TR, nc). R is
+// written on every rank.
+struct TsqrShard {
+    int rank = 0, size = 1;
+    i64 T = 0, maxt = 0;
+    const i64* t0 = nullptr;   // first tile of each rank
+    const i64* nt = nullptr;   // tiles of each rank
+    double* mine = nullptr;
+    double* all = nullptr;
+    ShardGatherFn gather = nullptr;
+    void* ctx = nullptr;
+};
+int launch_tsqr_sharded(double* X, i64 ld, i64 m_local, int c0, int nc, double* R, int ldR, double* ws,
+                        const TsqrShard& sh, cudaStream_t st);
+
+// Gram partials only: part[c][i + j*na] = rows [c*rows, (c+1)*rows) of
+// X[:, a0:a0+na]^T X[:, b0:b0+nb], for the ceil(m / rows) chunks of exactly
+// `rows` rows (a multiple of 32; the last chunk is cut at m).
+int launch_gram_partials_fp64(const double* X, i64 ld, i64 m, int a0, int na, int b0, int nb, double* part,
+                              i64 rows, cudaStream_t st);
+
 // Accuracy metrics (the reference's test_orth_accuracy, SRC/util.c:36-75).
 // E (n x n, lde) = G - I from the upper triangle of the Gram G (ld ldg), mirrored;
 // out[0] = ||E||_F (double-double accumulation, fixed order).

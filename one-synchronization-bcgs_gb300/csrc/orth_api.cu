@@ -323,6 +323,54 @@ struct HostLink {
 };
 
 // ---------------------------------------------------------------------------
+// Row-sharded runs: this rank holds rows [row0, row0 + msub) of X. The Gram's
+// partial sums are taken over chunks of kShardRows rows, aligned globally; every
+// rank gathers all ranks' chunk partials (in rank order, padded to maxc chunks
+// with zeros) and sums them in global chunk order, so every rank gets the Gram a
+// one-rank run of the same chunking gets, bit for bit. TSQR gathers its leaf
+// level's R factors the same way (TsqrShard).
+// ---------------------------------------------------------------------------
+constexpr i64 kShardRows = ORTH_GB300_SHARD_ROWS;
+
+struct Shard {
+    const orth_gb300_comm* comm = nullptr;
+    int rank = 0, size = 1;
+    i64 row0 = 0, msub = 0, m = 0;
+    i64 maxc = 0;                    // most Gram chunks on any rank
+    std::vector<i64> t0, nt;         // TSQR leaf tiles of each rank
+    i64 T = 0, maxt = 0;
+    DevBuf part, all, tmine, tall;   // exchange buffers
+};
+
+// The reference's 1-D block-row partition (SRC/orth.c:69-76, TESTS/test_orth.c:
+// 24-32) applied to chunks of kShardRows rows: size ranks share ceil(m / rows)
+// chunks, each rank m/size of them and the last (m mod size) ranks one more.
+void shard_chunks(i64 m, int size, int rank, i64* c_begin, i64* c_count) {
+    const i64 nch = ceil_div(m, kShardRows);
+    const i64 cpr = nch / size, res = nch - cpr * size;
+    if (res >= size - rank) {
+        *c_begin = rank * cpr + res - size + rank;
+        *c_count = cpr + 1;
+    } else {
+        *c_begin = rank * cpr;
+        *c_count = cpr;
+    }
+}
+
+void shard_rows(i64 m, int size, int rank, i64* row0, i64* msub) {
+    i64 cb = 0, cc = 0;
+    shard_chunks(m, size, rank, &cb, &cc);
+    *row0 = cb * kShardRows;
+    const i64 end = (cb + cc) * kShardRows < m ? (cb + cc) * kShardRows : m;
+    *msub = end > *row0 ? end - *row0 : 0;
+}
+
+int comm_gather(void* ctx, const double* mine, double* all, long long count, cudaStream_t st) {
+    const orth_gb300_comm* c = static_cast<const orth_gb300_comm*>(ctx);
+    return c->allgather(c->ctx, mine, all, count, (void*)st) ? (int)cudaErrorUnknown : 0;
+}
+
+// ---------------------------------------------------------------------------
 // Per-call engine: the primitives every variant is written in.
 // ---------------------------------------------------------------------------
 struct Engine {
@@ -338,6 +386,26 @@ struct Engine {
     int* status;
     int err = 0;
     HostLink* link = nullptr;   // host-buffer runs only
+    Shard* shard = nullptr;     // row-sharded runs only (FP64)
+
+    // C (na x nb, ldc) = X[:, a0:a0+na]^T X[:, b0:b0+nb] in FP64: one deterministic
+    // reduction, over all ranks in a row-sharded run.
+    void gram_fp64(int a0, int na, int b0, int nb, double* C, int ldc) {
+        if (err) return;
+        if (!shard) {
+            const int chunks = gram_chunks_fp64(m, na, nb, g_ctx.num_sms);
+            err = launch_gram_fp64(X, ld, m, a0, na, b0, nb, C, ldc, scr().part.as<double>(), chunks, st);
+            return;
+        }
+        Shard& sh = *shard;
+        const i64 blk = (i64)na * nb;
+        const i64 mine = ceil_div(m, kShardRows);
+        double* part = sh.part.as<double>();
+        err = launch_gram_partials_fp64(X, ld, m, a0, na, b0, nb, part, kShardRows, st);
+        if (!err && mine < sh.maxc) err = zero_async(part + mine * blk, (size_t)((sh.maxc - mine) * blk) * sizeof(double), st);
+        if (!err) err = comm_gather((void*)sh.comm, part, sh.all.as<double>(), sh.maxc * blk, st);
+        if (!err) err = launch_gram_reduce(sh.all.as<double>(), (int)(sh.size * sh.maxc), na, nb, C, ldc, st);
+    }
 
     // X columns [0, c_end) must be on the device; columns [0, c_fin) are final.
     void host_sync(int c_end, int c_fin) {
@@ -363,8 +431,7 @@ struct Engine {
                                     scr().split.bytes, g_ctx.num_sms, st);
             return;
         }
-        int chunks = gram_chunks_fp64(m, na, nb, g_ctx.num_sms);
-        err = launch_gram_fp64(X, ld, m, 0, na, b0, nb, C, na, scr().part.as<double>(), chunks, st);
+        gram_fp64(0, na, b0, nb, C, na);
     }
     // X[:, c0:c0+nc] = (X[:, c0:c0+nc] - X[:, 0:K] S) T^{-1}
     void update(int K, int c0, int nc, const double* S, int lds, const double* T, int ldt) {
@@ -422,6 +489,15 @@ struct Engine {
         if (err) return;
         host_sync(c0 + nc, c0);
         ProfScope ps(3, st, 6.0 * m * nc * nc, 8.0 * m * nc * 3.0);
+        if (shard) {
+            TsqrShard ts;
+            ts.rank = shard->rank; ts.size = shard->size; ts.T = shard->T; ts.maxt = shard->maxt;
+            ts.t0 = shard->t0.data(); ts.nt = shard->nt.data();
+            ts.mine = shard->tmine.as<double>(); ts.all = shard->tall.as<double>();
+            ts.gather = comm_gather; ts.ctx = (void*)shard->comm;
+            err = launch_tsqr_sharded(X, ld, m, c0, nc, Rout, ldr, scr().tsqr.as<double>(), ts, st);
+            return;
+        }
         err = launch_tsqr(X, ld, m, c0, nc, Rout, ldr, scr().tsqr.as<double>(), st);
         if (is_split(precision)) split_mark_stale(c0, nc);
     }
@@ -437,8 +513,7 @@ struct Engine {
         double* R2 = R1 + (i64)s * s;
         for (int pass = 0; pass < 2 && !err; ++pass) {
             double* T = pass ? R2 : R1;
-            err = launch_gram_fp64(X, ld, m, c0, nc, c0, nc, G, nc, scr().part.as<double>(),
-                                   gram_chunks_fp64(m, nc, nc, g_ctx.num_sms), st);
+            gram_fp64(c0, nc, c0, nc, G, nc);
             if (!err) err = launch_pyth_chol(G, nc, nullptr, 0, 0, nc, T, nc, status, step, st);
             if (!err) err = launch_update_fp64(X, ld, m, 0, 0, c0, nc, nullptr, 0, T, nc, st);
         }
@@ -770,6 +845,73 @@ int run_device(int variant, int m, int n, int s, double* dX, i64 ldX, double* dR
     return e.err ? 3 : 0;
 }
 
+// Row-sharded run of one rank (FP64): this rank's rows of X (msub x n, ld ldX)
+// and a full R (written on every rank, as the reference writes R on every rank).
+int run_sharded(int variant, i64 m, int n, int s, double* dX, i64 ldX, double* dR, int ldR, cudaStream_t st,
+                const orth_gb300_comm* comm, orth_gb300_status* out) {
+    if (out) std::memset(out, 0, sizeof(*out));
+    if (!comm || !comm->allgather || comm->size < 1 || comm->rank < 0 || comm->rank >= comm->size) return 2;
+    if (variant < 0 || variant > 4 || s < 1 || s > 64 || n < 2 * s || ldR < n || m < n || !dX || !dR) return 2;
+    if (ceil_div(m, kShardRows) < comm->size) return 2;   // every rank holds at least one chunk
+    Shard sh;
+    sh.comm = comm; sh.rank = comm->rank; sh.size = comm->size; sh.m = m;
+    shard_rows(m, sh.size, sh.rank, &sh.row0, &sh.msub);
+    if (ldX < sh.msub) return 2;
+    const int TR = tsqr_tile_rows(s);
+    sh.t0.resize(sh.size); sh.nt.resize(sh.size);
+    for (int r = 0; r < sh.size; ++r) {
+        i64 r0 = 0, ms = 0, cb = 0, cc = 0;
+        shard_rows(m, sh.size, r, &r0, &ms);
+        shard_chunks(m, sh.size, r, &cb, &cc);
+        sh.t0[r] = r0 / TR;
+        sh.nt[r] = ceil_div(ms, TR);
+        if (cc > sh.maxc) sh.maxc = cc;
+        if (sh.nt[r] > sh.maxt) sh.maxt = sh.nt[r];
+    }
+    sh.T = ceil_div(m, TR);
+    int rc = init_ctx();
+    if (!rc) rc = reserve(sh.msub, n, s, ORTH_GB300_FP64);
+    const i64 blk = (i64)(n + s) * 2 * s;
+    if (!rc) rc = sh.part.ensure((size_t)(sh.maxc * blk) * sizeof(double));
+    if (!rc) rc = sh.all.ensure((size_t)(sh.size * sh.maxc * blk) * sizeof(double));
+    if (!rc) rc = sh.tmine.ensure((size_t)(sh.maxt * s * s) * sizeof(double));
+    if (!rc) rc = sh.tall.ensure((size_t)(sh.size * sh.maxt * s * s) * sizeof(double));
+    if (!rc) rc = scr().tsqr.ensure((size_t)tsqr_workspace_doubles(m, s) * sizeof(double));
+    if (rc) {
+        if (out) out->cuda_error = rc;
+        return 3;
+    }
+    const long long reductions0 = g_reduce_count;
+    Engine e{dX, ldX, sh.msub, n, s, dR, ldR, ORTH_GB300_FP64, st,
+             carve_small(scr().small.as<double>(), n, s), scr().status.as<int>()};
+    e.shard = &sh;
+    e.err = zero_async(e.status, kStatusWords * sizeof(int), st);
+    switch (variant) {
+        case ORTH_GB300_BCGSI2P1S: run_p1s(e); break;
+        case ORTH_GB300_BCGSI21S: run_21s(e); break;
+        case ORTH_GB300_BCGSPIPI2: run_pipi(e); break;
+        case ORTH_GB300_BCGSI2: run_bcgsi2(e); break;
+        default: run_p2s(e); break;
+    }
+    g_last_reductions = g_reduce_count - reductions0;
+    int h[kStatusWords] = {0, 0, 0, 0};
+    if (!e.err) {
+        cudaError_t ce = cudaMemcpyAsync(h, e.status, sizeof(h), cudaMemcpyDeviceToHost, st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+        if (ce != cudaSuccess) e.err = (int)ce;
+    }
+    if (out) {
+        out->breakdown_step = h[0];
+        out->breakdown_info = h[1];
+        out->timeout = h[2];
+        out->cuda_error = e.err;
+    }
+    // The exchange buffers are this call's: wait for the stream before they go.
+    cudaStreamSynchronize(st);
+    sh.part.release(); sh.all.release(); sh.tmine.release(); sh.tall.release();
+    return e.err ? 3 : 0;
+}
+
 // Whether p is memory the GPU can address directly (device or managed memory).
 bool is_device_pointer(const void* p) {
     cudaPointerAttributes a;
@@ -1092,6 +1234,21 @@ int orth_gb300_set_host_precision(int precision) {
 }
 
 int orth_gb300_last_split_error(void) { return split_last_error(); }
+
+int orth_gb300_shard_rows(long long m, int size, int rank, long long* row0, long long* msub) {
+    if (m < 1 || size < 1 || rank < 0 || rank >= size || !row0 || !msub) return 2;
+    i64 r0 = 0, ms = 0;
+    shard_rows(m, size, rank, &r0, &ms);
+    *row0 = r0;
+    *msub = ms;
+    return ceil_div(m, kShardRows) < size ? 2 : 0;
+}
+
+int orth_gb300_run_sharded(int variant, long long m, int n, int s, double* dXsub, long long ldX, double* dR,
+                           int ldR, void* stream, const orth_gb300_comm* comm, orth_gb300_status* status) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    return run_sharded(variant, m, n, s, dXsub, ldX, dR, ldR, (cudaStream_t)stream, comm, status);
+}
 
 int orth_gb300_set_intra_ortho(int mode) {
     if (mode != ORTH_GB300_INTRA_TSQR && mode != ORTH_GB300_INTRA_CHOLQR2) return 2;

@@ -463,21 +463,19 @@ __device__ __forceinline__ double assemble(long long hi, long long mid, float lo
 }
 
 // Producer: for each chunk, B planes then KD A planes (TMA), each with its L2
-// eviction policy (polA, polB). The coordinate function also gives `pieces`:
-// 0 loads the whole A box through mapA; k > 0 loads only k 16-column pieces
-// through mapP (box {64, 16, 1}), so that a partial M-block (Gram) or a partial
-// last K chunk (update) does not read the columns past the operand's end. A
-// piece p of half h lands where the whole box would put it: h * 8 KB + p * 2 KB
-// (halves = 2: the update's two 64-row chunks).
+// eviction policy (polA, polB). The coordinate function also picks the A map
+// and the bytes its box holds: the update's last K chunk uses a map whose box
+// covers only the chunk's valid columns, so it does not read past kin.
 template <int NB, int KD, class CoordFn>
-__device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapA, const CUtensorMap* mapP, const CUtensorMap* mapB,
-                                              uint8_t* sA, uint8_t* sB, Bars* bars, Ring& ra, Ring& rb, CoordFn coords,
-                                              int item, int ch, volatile int* abort, int* err, uint64_t polA,
-                                              uint64_t polB, int halves) {
+__device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapB, uint8_t* sA, uint8_t* sB, Bars* bars,
+                                              Ring& ra, Ring& rb, CoordFn coords, int item, int ch,
+                                              volatile int* abort, int* err, uint64_t polA, uint64_t polB) {
     constexpr int B_SLOT = SmemLayout<NB, KD>::B_SLOT;
     // Plane p of A is at (ax, ay, az + p*azs); plane p of B at (bx, by, bz + p*bzs).
-    int ax, ay, az, azs, bx, by, bz, bzs, pieces;
-    coords(item, ch, ax, ay, az, azs, bx, by, bz, bzs, pieces);
+    int ax, ay, az, azs, bx, by, bz, bzs;
+    uint32_t abytes;
+    const CUtensorMap* mapA;
+    coords(item, ch, ax, ay, az, azs, bx, by, bz, bzs, mapA, abytes);
     if (!tc::mbar_wait(&bars->b_empty[rb.slot], rb.phase ^ 1u, abort, err, 11)) return false;
     tc::mbar_expect_tx(&bars->b_full[rb.slot], (uint32_t)B_SLOT);
 #pragma unroll
@@ -485,31 +483,25 @@ __device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapA, const CUt
         tc::tma_load_3d_hint(sB + rb.slot * B_SLOT + j * NB * KCH * 2, mapB, &bars->b_full[rb.slot], bx, by,
                              bz + j * bzs, polB);
     rb.advance(RB);
-    const uint32_t abytes = pieces ? (uint32_t)(halves * pieces * 2048) : (uint32_t)A_SLOT;
 #pragma unroll
     for (int i = 0; i < KD; ++i) {
         if (!tc::mbar_wait(&bars->a_empty[ra.slot], ra.phase ^ 1u, abort, err, 12 + 100 * ra.slot)) return false;
         tc::mbar_expect_tx(&bars->a_full[ra.slot], abytes);
-        uint8_t* dst = sA + ra.slot * A_SLOT;
-        if (!pieces) {
-            tc::tma_load_3d_hint(dst, mapA, &bars->a_full[ra.slot], ax, ay, az + i * azs, polA);
-        } else {
-            for (int h = 0; h < halves; ++h)
-                for (int q = 0; q < pieces; ++q)
-                    tc::tma_load_3d_hint(dst + h * 8192 + q * 2048, mapP, &bars->a_full[ra.slot], ax, ay + 16 * q,
-                                         az + h + i * azs, polA);
-        }
+        tc::tma_load_3d_hint(sA + ra.slot * A_SLOT, mapA, &bars->a_full[ra.slot], ax, ay, az + i * azs, polA);
         ra.advance(RA);
     }
     return true;
 }
 
 // MMA issuer for one chunk into TMEM buffer `dcol` (column offset). A_MN: the A
-// tile is two 64-row blocks (LBO 8 KB apart) of 64 K-rows of 128 bytes (MN-major).
+// tile is two 64-row blocks (LBO apart: 8 KB for a whole chunk, kv * 128 bytes
+// for a last chunk of kv columns) of K-rows of 128 bytes (MN-major); only the
+// first ksteps 16-row K steps are issued.
 template <int NB, int KD, bool A_MN = false>
 __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uint8_t* sA, uint8_t* sB,
                                           Bars* bars, Ring& ra, Ring& rb, bool first_in_window,
-                                          volatile int* abort, int* err, int ksteps = KCH / 16) {
+                                          volatile int* abort, int* err, int ksteps = KCH / 16,
+                                          uint32_t lbo = 64 * KCH * 2) {
     constexpr int B_SLOT = SmemLayout<NB, KD>::B_SLOT;
     if (!tc::mbar_wait(&bars->b_full[rb.slot], rb.phase, abort, err, 21)) return false;
     const uint32_t b_addr = tc::smem_u32(sB + rb.slot * B_SLOT);
@@ -523,7 +515,7 @@ __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uin
 #pragma unroll
         for (int k = 0; k < KCH / 16; ++k) {
             if (k >= ksteps) break;
-            const uint64_t da = A_MN ? tc::sw128_desc_mn(a_addr + k * 16 * 128, 64 * KCH * 2)
+            const uint64_t da = A_MN ? tc::sw128_desc_mn(a_addr + k * 16 * 128, lbo)
                                      : tc::sw128_desc(a_addr + k * 32);
             const uint64_t db = tc::sw128_desc(b_addr + k * 32);
             const uint32_t acc = (first_in_window && i == 0 && k == 0) ? 0u : 1u;
@@ -578,8 +570,7 @@ struct GramParams {
 
 template <int KD>
 __global__ void __launch_bounds__(NTHREADS, 1)
-gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapP,
-               const __grid_constant__ CUtensorMap mapB, GramParams p) {
+gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GramParams p) {
     constexpr int NB = 32;
     using L = SmemLayout<NB, KD>;
     extern __shared__ uint8_t smem_raw[];
@@ -600,16 +591,13 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     const int nchunks = r1 > r0 ? (int)ceil_div(r1 - r0, KCH) : 0;
     const int nwin = (nchunks + WIN - 1) / WIN;
 
-    // A partial last M-block loads only its columns, in 16-column pieces; the
-    // tile's other rows keep stale data and give D rows that are not written.
-    const int va = min(TILE_M, p.na - mb * TILE_M);
-    const int apieces = va >= TILE_M ? 0 : (va + 15) / 16;
     auto coords = [&](int, int ch, int& ax, int& ay, int& az, int& azs, int& bx, int& by, int& bz, int& bzs,
-                      int& pieces) {
+                      const CUtensorMap*& amap, uint32_t& abytes) {
         const int rc = (int)((r0 + (i64)ch * KCH) / KCH);   // 64-row chunk of the column store
         ax = 0; ay = mb * TILE_M; az = rc; azs = p.nrc;
         bx = 0; by = p.b0 + ng * NB; bz = rc; bzs = p.nrc;
-        pieces = apieces;
+        amap = &mapA;
+        abytes = (uint32_t)A_SLOT;
     };
 
     if (warp == 0) {
@@ -620,8 +608,8 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
             const uint64_t polB = tc::policy_evict_last();
             Ring ra, rb;
             for (int ch = 0; ch < nchunks; ++ch)
-                if (!produce_chunk<NB, KD>(&mapA, &mapP, &mapB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag,
-                                           p.err, polA, polB, 1))
+                if (!produce_chunk<NB, KD>(&mapB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag, p.err, polA,
+                                           polB))
                     break;
             if (abort_flag) {
                 drain_ring(bars->a_full, RA, ra);
@@ -709,7 +697,8 @@ struct UpdateParams {
 
 template <int NB, int KD>
 __global__ void __launch_bounds__(NTHREADS, 1)
-update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapP,
+update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapA16,
+                 const __grid_constant__ CUtensorMap mapA32, const __grid_constant__ CUtensorMap mapA48,
                  const __grid_constant__ CUtensorMap mapB, UpdateParams p) {
     using L = SmemLayout<NB, KD>;
     extern __shared__ uint8_t smem_raw[];
@@ -728,15 +717,18 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     if (threadIdx.x < 32) s_cmax[threadIdx.x] = 0ULL;
     __syncthreads();
 
-    // The last K chunk loads only its kin - ch * KCH columns (16-column pieces)
-    // and issues only their MMA K steps.
-    auto kvalid = [&](int ch) { return min(KCH, p.kin - ch * KCH); };
+    // The last K chunk loads only its kv = kin - ch * KCH columns, rounded up to 16
+    // (a box of kv columns x two 64-row chunks; the second chunk lands kv * 128
+    // bytes after the first), and issues only their MMA K steps.
+    const int kv_last = p.kin - (nchunks - 1) * KCH;
+    const int kr_last = (kv_last + 15) / 16 * 16;   // 16, 32, 48 or 64
     auto coords = [&](int tile, int ch, int& ax, int& ay, int& az, int& azs, int& bx, int& by, int& bz, int& bzs,
-                      int& pieces) {
+                      const CUtensorMap*& amap, uint32_t& abytes) {
         ax = 0; ay = ch * KCH; az = 2 * tile; azs = p.nrc;   // 64 columns x two 64-row chunks
         bx = ch * KCH; by = 0; bz = 0; bzs = 1;
-        const int kv = kvalid(ch);
-        pieces = kv >= KCH ? 0 : (kv + 15) / 16;
+        const int kr = ch == nchunks - 1 ? kr_last : KCH;
+        amap = kr == 16 ? &mapA16 : (kr == 32 ? &mapA32 : (kr == 48 ? &mapA48 : &mapA));
+        abytes = (uint32_t)(kr * 256);
     };
 
     // Row tiles are handed out dynamically: the producer takes the next tile number
@@ -760,8 +752,8 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
                 rq.advance(RQ);
                 if (tile >= ntiles) break;
                 for (int ch = 0; ch < nchunks && ok; ++ch)
-                    ok = produce_chunk<NB, KD>(&mapA, &mapP, &mapB, sA, sB, bars, ra, rb, coords, tile, ch,
-                                               &abort_flag, p.err, polA, polB, 2);
+                    ok = produce_chunk<NB, KD>(&mapB, sA, sB, bars, ra, rb, coords, tile, ch, &abort_flag, p.err,
+                                               polA, polB);
             }
             if (abort_flag) {
                 drain_ring(bars->a_full, RA, ra);
@@ -785,9 +777,12 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
                     if (!tc::mbar_wait(&bars->t_empty[buf], tph ^ 1u, &abort_flag, p.err, 32)) { ok = false; break; }
                     tc::tc_fence_after();
                     const int c_end = min(nchunks, (w + 1) * WIN);
-                    for (int ch = w * WIN; ch < c_end && ok; ++ch)
+                    for (int ch = w * WIN; ch < c_end && ok; ++ch) {
+                        const int kr = ch == nchunks - 1 ? kr_last : KCH;
                         ok = mma_chunk<NB, KD, true>(tmem, (uint32_t)(buf * L::TMEM_COLS_PER_BUF), sA, sB, bars, ra,
-                                                     rb, ch == w * WIN, &abort_flag, p.err, (kvalid(ch) + 15) / 16);
+                                                     rb, ch == w * WIN, &abort_flag, p.err, kr / 16,
+                                                     (uint32_t)(kr * 128));
+                    }
                     if (ok) tc::mma_commit(&bars->t_full[buf]);
                 }
             }
@@ -905,7 +900,7 @@ struct Plan {
     double *bfull = nullptr, *part = nullptr;
     i64 part_doubles = 0;
     // maps
-    CUtensorMap map_col_a, map_col_b, map_col_u, map_col_p, map_bdig16, map_bdig32;
+    CUtensorMap map_col_a, map_col_b, map_col_u, map_col_u16, map_col_u32, map_col_u48, map_bdig16, map_bdig32;
     int kd = 7;
     std::vector<char> fresh;
     std::vector<char> cmax_valid;   // cmax[c] already holds max |X[:, c]| (set by the update)
@@ -1041,8 +1036,10 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     if (!rc) rc = make_map3(&P.map_col_b, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 32);
     // Update A tiles: 64 columns of two adjacent 64-row chunks (128 rows).
     if (!rc) rc = make_map3(&P.map_col_u, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, KCH, 2);
-    // 16-column pieces (one 64-row chunk): partial Gram M-blocks, partial update K chunks.
-    if (!rc) rc = make_map3(&P.map_col_p, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 16, 1);
+    // The update's last K chunk when kin is not a multiple of 64: 16, 32 or 48 columns.
+    if (!rc) rc = make_map3(&P.map_col_u16, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 16, 2);
+    if (!rc) rc = make_map3(&P.map_col_u32, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 32, 2);
+    if (!rc) rc = make_map3(&P.map_col_u48, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 48, 2);
     if (!rc) rc = make_map3(&P.map_bdig16, P.bdig, P.kpad, 16, KD_MAX, P.kpad, 16 * P.kpad, 16);
     if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
     if (rc) return rc;
@@ -1118,8 +1115,8 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     gp.a_once = gp.numNG == 1 ? 1 : 0;
     const unsigned grid = (unsigned)(mbn * gp.rc);
     const int smem = P.kd == 6 ? SmemLayout<32, 6>::BYTES : SmemLayout<32, 7>::BYTES;
-    if (P.kd == 6) gram_tc_kernel<6><<<grid, NTHREADS, smem, st>>>(P.map_col_a, P.map_col_p, P.map_col_b, gp);
-    else gram_tc_kernel<7><<<grid, NTHREADS, smem, st>>>(P.map_col_a, P.map_col_p, P.map_col_b, gp);
+    if (P.kd == 6) gram_tc_kernel<6><<<grid, NTHREADS, smem, st>>>(P.map_col_a, P.map_col_b, gp);
+    else gram_tc_kernel<7><<<grid, NTHREADS, smem, st>>>(P.map_col_a, P.map_col_b, gp);
     g_launch_count += 1;
     rc = (int)cudaGetLastError();
     if (rc) return rc;
@@ -1156,8 +1153,8 @@ static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int 
         const int ntiles = (int)ceil_div(m, TILE_M);
         const int grid = ntiles < num_sms ? ntiles : num_sms;
 #define BCGS_UPD(NBT, KDT) \
-        update_tc_kernel<NBT, KDT><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(P.map_col_u, P.map_col_p, \
-                                                                                         P.map_bdig##NBT, up)
+        update_tc_kernel<NBT, KDT><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(                        \
+            P.map_col_u, P.map_col_u16, P.map_col_u32, P.map_col_u48, P.map_bdig##NBT, up)
         if (NB == 16) {
             if (P.kd == 6) BCGS_UPD(16, 6); else BCGS_UPD(16, 7);
         } else {

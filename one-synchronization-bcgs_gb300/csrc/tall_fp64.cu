@@ -166,6 +166,17 @@ int launch_gram_fp64(const double* X, i64 ld, i64 m, int a0, int na, int b0, int
     return (int)cudaGetLastError();
 }
 
+int launch_gram_partials_fp64(const double* X, i64 ld, i64 m, int a0, int na, int b0, int nb, double* part,
+                              i64 rows, cudaStream_t st) {
+    if (na <= 0 || nb <= 0 || m <= 0) return 0;
+    if (rows <= 0 || rows % GT_R != 0) return (int)cudaErrorInvalidValue;
+    const i64 nchunks = ceil_div(m, rows);
+    dim3 grid((unsigned)nchunks, (unsigned)ceil_div(na, GT_A), (unsigned)ceil_div(nb, GT_B));
+    gram_fp64_partial<<<grid, GT_THREADS, 0, st>>>(X, ld, m, a0, na, b0, nb, rows, part);
+    g_launch_count += 1;
+    return (int)cudaGetLastError();
+}
+
 int launch_gram_reduce(const double* part, int nchunks, int na, int nb, double* out, int ldo,
                        cudaStream_t st) {
     const i64 total = (i64)na * nb;

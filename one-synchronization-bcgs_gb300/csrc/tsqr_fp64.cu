@@ -295,20 +295,22 @@ i64 tsqr_workspace_doubles(i64 m, int nc) {
     return total + 64 * 64;  // + the root tile's R
 }
 
+// The tree from a given level on: level 0 here is (A0, rows0, ld0), factored in
+// place; each level's tile R factors are stacked into the next level (in ws),
+// until one tile remains (the root). Then the root's signs are fixed, R is
+// written to (R, ldR), and the down-sweep brings the explicit Q back to level 0.
 template <int NC>
-static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR, double* ws,
-                    cudaStream_t st) {
+static int tsqr_levels(double* A0, i64 ld0, i64 rows0, int nc, double* R, int ldR, double* ws, cudaStream_t st) {
     const int TR = tsqr_tile_rows(nc);
     const size_t smem = tsqr_tile_smem_bytes(TR, NC);
     const int attr_rc = smem_attr((const void*)tsqr_tile_kernel<NC>, (int)smem);
     if (attr_rc) return attr_rc;
-    // Level matrices: level 0 is the panel itself; level l >= 1 lives in ws.
     constexpr int kMaxLevels = 48;   // each level divides the rows by TR / nc >= 2: 2^k rows need at most k levels
     double* lvl_ptr[kMaxLevels];
     i64 lvl_rows[kMaxLevels], lvl_ld[kMaxLevels];
-    lvl_ptr[0] = X + (i64)c0 * ld;
-    lvl_rows[0] = m;
-    lvl_ld[0] = ld;
+    lvl_ptr[0] = A0;
+    lvl_rows[0] = rows0;
+    lvl_ld[0] = ld0;
     int L = 0;
     double* cursor = ws;
     while (lvl_rows[L] > TR) {
@@ -338,6 +340,69 @@ static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR
         g_launch_count += 1;
     }
     return (int)cudaGetLastError();
+}
+
+template <int NC>
+static int tsqr_run(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR, double* ws,
+                    cudaStream_t st) {
+    return tsqr_levels<NC>(X + (i64)c0 * ld, ld, m, nc, R, ldR, ws, st);
+}
+
+// Row-sharded TSQR: this rank's rows are the TR-row tiles [t0, t0 + nt) of a
+// panel of T tiles. The leaf level runs on the local tiles, writing their R
+// factors to `mine` (maxt * nc rows, ld maxt * nc); gather(mine, all) places every
+// rank's block in rank order; the blocks are assembled into the global level-1
+// stack (T * nc rows, as the one-rank tree has it), whose tree every rank runs;
+// the down-sweep of the local tiles then uses this rank's rows of level 1's Q.
+// With tiles aligned across ranks, every launch sees the data the one-rank TSQR
+// sees, so Q and R are bit-identical to it.
+template <int NC>
+static int tsqr_sharded_run(double* X, i64 ld, i64 m_local, int c0, int nc, double* R, int ldR, double* ws,
+                            const TsqrShard& sh, cudaStream_t st) {
+    const int TR = tsqr_tile_rows(nc);
+    const size_t smem = tsqr_tile_smem_bytes(TR, NC);
+    const int attr_rc = smem_attr((const void*)tsqr_tile_kernel<NC>, (int)smem);
+    if (attr_rc) return attr_rc;
+    if (sh.T <= 1) return tsqr_run<NC>(X, ld, m_local, c0, nc, R, ldR, ws, st);   // one tile: one rank holds it
+    double* panel = X + (i64)c0 * ld;
+    const i64 nt = ceil_div(m_local, TR);
+    const i64 ldm = sh.maxt * nc;
+    if (nt > 0) {
+        tsqr_tile_kernel<NC><<<(unsigned)nt, 32 * tsqr_tile_warps<NC>(), smem, st>>>(panel, ld, m_local, nc, panel, ld,
+                                                                                   sh.mine, ldm);
+        g_launch_count += 1;
+    }
+    int rc = (int)cudaGetLastError();
+    if (rc) return rc;
+    rc = sh.gather(sh.ctx, sh.mine, sh.all, ldm * nc, st);
+    if (rc) return rc;
+    double* lvl1 = ws;
+    const i64 ld1 = sh.T * nc;
+    for (int r = 0; r < sh.size; ++r) {
+        if (sh.nt[r] <= 0) continue;
+        rc = (int)cudaMemcpy2DAsync(lvl1 + sh.t0[r] * nc, (size_t)ld1 * sizeof(double), sh.all + (i64)r * ldm * nc,
+                                    (size_t)ldm * sizeof(double), (size_t)(sh.nt[r] * nc) * sizeof(double), (size_t)nc,
+                                    cudaMemcpyDeviceToDevice, st);
+        if (rc) return rc;
+    }
+    rc = tsqr_levels<NC>(lvl1, ld1, ld1, nc, R, ldR, ws + ld1 * nc, st);
+    if (rc) return rc;
+    if (nt > 0) {
+        tsqr_apply_kernel<NC><<<(unsigned)ceil_div(m_local, 128), 128, 0, st>>>(panel, ld, m_local, nc, TR,
+                                                                                 lvl1 + sh.t0[sh.rank] * nc, ld1);
+        g_launch_count += 1;
+    }
+    return (int)cudaGetLastError();
+}
+
+int launch_tsqr_sharded(double* X, i64 ld, i64 m_local, int c0, int nc, double* R, int ldR, double* ws,
+                        const TsqrShard& sh, cudaStream_t st) {
+    if (nc <= 0) return 0;
+    if (nc <= 8) return tsqr_sharded_run<8>(X, ld, m_local, c0, nc, R, ldR, ws, sh, st);
+    if (nc <= 16) return tsqr_sharded_run<16>(X, ld, m_local, c0, nc, R, ldR, ws, sh, st);
+    if (nc <= 32) return tsqr_sharded_run<32>(X, ld, m_local, c0, nc, R, ldR, ws, sh, st);
+    if (nc <= 64) return tsqr_sharded_run<64>(X, ld, m_local, c0, nc, R, ldR, ws, sh, st);
+    return (int)cudaErrorInvalidValue;
 }
 
 int launch_tsqr(double* X, i64 ld, i64 m, int c0, int nc, double* R, int ldR, double* ws,
