@@ -82,7 +82,8 @@ int launch_tsqr_sharded(double* X, i64 ld, i64 m_local, int c0, int nc, double* 
 
 // Gram partials only: part[c][i + j*na] = rows [c*rows, (c+1)*rows) of
 // X[:, a0:a0+na]^T X[:, b0:b0+nb], for the ceil(m / rows) chunks of exactly
-// `rows` rows (a multiple of 32; the last chunk is cut at m).
+// `rows` rows (a multiple of 32; the last chunk is cut at m). Each chunk is summed
+// in segments of 256 rows, so accuracy does not degrade with `rows`.
 int launch_gram_partials_fp64(const double* X, i64 ld, i64 m, int a0, int na, int b0, int nb, double* part,
                               i64 rows, cudaStream_t st);
 

@@ -560,6 +560,7 @@ __device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint
 struct GramParams {
     int na, nb, b0, nrc;
     int a_once;      // 1: every A tile is read by one CTA only (numNG == 1), loaded evict_first
+    int alast;       // columns the last M-block's A box holds (na - 128 (numMB - 1), rounded up to 16)
     i64 m;
     int numMB, numNG, rc;
     i64 rows_per;   // multiple of WIN*KCH
@@ -570,7 +571,8 @@ struct GramParams {
 
 template <int KD>
 __global__ void __launch_bounds__(NTHREADS, 1)
-gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GramParams p) {
+gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapAlast,
+               const __grid_constant__ CUtensorMap mapB, GramParams p) {
     constexpr int NB = 32;
     using L = SmemLayout<NB, KD>;
     extern __shared__ uint8_t smem_raw[];
@@ -591,13 +593,17 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     const int nchunks = r1 > r0 ? (int)ceil_div(r1 - r0, KCH) : 0;
     const int nwin = (nchunks + WIN - 1) / WIN;
 
+    // The last M-block, when na is not a multiple of 128, loads only its
+    // p.alast columns (mapAlast's box); the tile's other rows keep stale data
+    // and give D rows that are not written.
+    const bool last_part = mb == p.numMB - 1 && p.alast < TILE_M;
     auto coords = [&](int, int ch, int& ax, int& ay, int& az, int& azs, int& bx, int& by, int& bz, int& bzs,
                       const CUtensorMap*& amap, uint32_t& abytes) {
         const int rc = (int)((r0 + (i64)ch * KCH) / KCH);   // 64-row chunk of the column store
         ax = 0; ay = mb * TILE_M; az = rc; azs = p.nrc;
         bx = 0; by = p.b0 + ng * NB; bz = rc; bzs = p.nrc;
-        amap = &mapA;
-        abytes = (uint32_t)A_SLOT;
+        amap = last_part ? &mapAlast : &mapA;
+        abytes = last_part ? (uint32_t)(p.alast * KCH * 2) : (uint32_t)A_SLOT;
     };
 
     if (warp == 0) {
@@ -690,15 +696,16 @@ struct UpdateParams {
     i64 ld;
     double* X;
     const int* fexp;
-    unsigned long long* cmax;   // column max |X[:, c0 + j]| of the written block (bit patterns)
+    unsigned long long* cmax;   // column max |X[:, c0 + j]| of the written block (bit patterns; the
+                                // high word only, which holds the exponent the digit scale uses)
     int* err;
     int* tile_ctr;              // zeroed before the launch; CTAs take row tiles from it
+    int kr_last;                // columns the last K chunk's A box holds: kin - 64 (chunks - 1) rounded up to 16
 };
 
 template <int NB, int KD>
 __global__ void __launch_bounds__(NTHREADS, 1)
-update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapA16,
-                 const __grid_constant__ CUtensorMap mapA32, const __grid_constant__ CUtensorMap mapA48,
+update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapAlast,
                  const __grid_constant__ CUtensorMap mapB, UpdateParams p) {
     using L = SmemLayout<NB, KD>;
     extern __shared__ uint8_t smem_raw[];
@@ -720,15 +727,14 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     // The last K chunk loads only its kv = kin - ch * KCH columns, rounded up to 16
     // (a box of kv columns x two 64-row chunks; the second chunk lands kv * 128
     // bytes after the first), and issues only their MMA K steps.
-    const int kv_last = p.kin - (nchunks - 1) * KCH;
-    const int kr_last = (kv_last + 15) / 16 * 16;   // 16, 32, 48 or 64
+    const int kr_last = p.kr_last;   // 16, 32, 48 (mapAlast's box) or 64
     auto coords = [&](int tile, int ch, int& ax, int& ay, int& az, int& azs, int& bx, int& by, int& bz, int& bzs,
                       const CUtensorMap*& amap, uint32_t& abytes) {
         ax = 0; ay = ch * KCH; az = 2 * tile; azs = p.nrc;   // 64 columns x two 64-row chunks
         bx = ch * KCH; by = 0; bz = 0; bzs = 1;
-        const int kr = ch == nchunks - 1 ? kr_last : KCH;
-        amap = kr == 16 ? &mapA16 : (kr == 32 ? &mapA32 : (kr == 48 ? &mapA48 : &mapA));
-        abytes = (uint32_t)(kr * 256);
+        const bool last = ch == nchunks - 1 && kr_last < KCH;
+        amap = last ? &mapAlast : &mapA;
+        abytes = (uint32_t)((last ? kr_last : KCH) * 256);
     };
 
     // Row tiles are handed out dynamically: the producer takes the next tile number
@@ -796,6 +802,12 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
         int wc = 0;
         bool ok = true;
         Ring rq;
+        // Running max over this thread's rows of the high word of |x| per output
+        // column: the digit scale needs only the exponent of the column max, which
+        // the high word holds. Reduced over the CTA once, after the last tile.
+        uint32_t rmax[NH];
+#pragma unroll
+        for (int jj = 0; jj < NH; ++jj) rmax[jj] = 0u;
         while (ok) {
             int tile = 0;
             if (lane == 0) {
@@ -828,20 +840,25 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
 #pragma unroll
             for (int jj = 0; jj < NH; ++jj) {
                 const int j = half * NH + jj;
-                unsigned long long a = 0ULL;
                 if (j < p.nc && r < p.m) {
                     const double v = assemble(hi[jj], mid[jj], lo[jj], p.fexp[j] - 78);
                     xr[(i64)j * p.ld] = v;
-                    a = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
-                    if ((a >> 52) == 0x7FF) a = 0ULL;
+                    uint32_t a = (uint32_t)((unsigned long long)__double_as_longlong(v) >> 32) & 0x7FFFFFFFu;
+                    if ((a >> 20) == 0x7FFu) a = 0u;   // Inf/NaN do not set the scale
+                    rmax[jj] = a > rmax[jj] ? a : rmax[jj];
                 }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const unsigned long long b = __shfl_xor_sync(0xffffffffu, a, o);
-                    a = a > b ? a : b;
-                }
-                if (lane == 0 && a) atomicMax(&s_cmax[j], a);
             }
+        }
+#pragma unroll
+        for (int jj = 0; jj < NH; ++jj) {
+            uint32_t a = rmax[jj];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const uint32_t b = __shfl_xor_sync(0xffffffffu, a, o);
+                a = a > b ? a : b;
+            }
+            const int j = half * NH + jj;
+            if (lane == 0 && a && j < p.nc) atomicMax(&s_cmax[j], (unsigned long long)a << 32);
         }
     }
     __syncthreads();
@@ -900,7 +917,9 @@ struct Plan {
     double *bfull = nullptr, *part = nullptr;
     i64 part_doubles = 0;
     // maps
-    CUtensorMap map_col_a, map_col_b, map_col_u, map_col_u16, map_col_u32, map_col_u48, map_bdig16, map_bdig32;
+    CUtensorMap map_col_a, map_col_b, map_col_u, map_bdig16, map_bdig32;
+    CUtensorMap map_col_a_part[7];   // Gram A boxes of 16, 32, ..., 112 columns (a partial last M-block)
+    CUtensorMap map_col_u_part[3];   // update A boxes of 16, 32, 48 columns x two 64-row chunks
     int kd = 7;
     std::vector<char> fresh;
     std::vector<char> cmax_valid;   // cmax[c] already holds max |X[:, c]| (set by the update)
@@ -1036,10 +1055,12 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     if (!rc) rc = make_map3(&P.map_col_b, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 32);
     // Update A tiles: 64 columns of two adjacent 64-row chunks (128 rows).
     if (!rc) rc = make_map3(&P.map_col_u, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, KCH, 2);
-    // The update's last K chunk when kin is not a multiple of 64: 16, 32 or 48 columns.
-    if (!rc) rc = make_map3(&P.map_col_u16, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 16, 2);
-    if (!rc) rc = make_map3(&P.map_col_u32, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 32, 2);
-    if (!rc) rc = make_map3(&P.map_col_u48, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 48, 2);
+    // Partial boxes: a Gram's last M-block of fewer than 128 columns, an update's
+    // last K chunk of fewer than 64 (in 16-column steps).
+    for (int q = 0; q < 7 && !rc; ++q)
+        rc = make_map3(&P.map_col_a_part[q], P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 16 * (q + 1));
+    for (int q = 0; q < 3 && !rc; ++q)
+        rc = make_map3(&P.map_col_u_part[q], P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 16 * (q + 1), 2);
     if (!rc) rc = make_map3(&P.map_bdig16, P.bdig, P.kpad, 16, KD_MAX, P.kpad, 16 * P.kpad, 16);
     if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
     if (rc) return rc;
@@ -1113,10 +1134,12 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     // (row range, N-group) are consecutive in blockIdx.x, so they run at the
     // same time and share each B tile through L2.
     gp.a_once = gp.numNG == 1 ? 1 : 0;
+    gp.alast = (int)round_up(na - (i64)(gp.numMB - 1) * TILE_M, 16);
+    const CUtensorMap& alast_map = gp.alast < TILE_M ? P.map_col_a_part[gp.alast / 16 - 1] : P.map_col_a;
     const unsigned grid = (unsigned)(mbn * gp.rc);
     const int smem = P.kd == 6 ? SmemLayout<32, 6>::BYTES : SmemLayout<32, 7>::BYTES;
-    if (P.kd == 6) gram_tc_kernel<6><<<grid, NTHREADS, smem, st>>>(P.map_col_a, P.map_col_b, gp);
-    else gram_tc_kernel<7><<<grid, NTHREADS, smem, st>>>(P.map_col_a, P.map_col_b, gp);
+    if (P.kd == 6) gram_tc_kernel<6><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp);
+    else gram_tc_kernel<7><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp);
     g_launch_count += 1;
     rc = (int)cudaGetLastError();
     if (rc) return rc;
@@ -1148,13 +1171,15 @@ static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int 
         up.nrc = (int)P.nrc;
         up.m = m; up.kin = kin; up.nc = ng; up.c0 = c0 + j0; up.ld = ld; up.X = X; up.fexp = P.fexp;
         up.cmax = P.cmax; up.err = P.err; up.tile_ctr = P.tile_ctr;
+        up.kr_last = (int)round_up(kin - (i64)(ceil_div(kin, KCH) - 1) * KCH, 16);
+        const CUtensorMap& ulast_map = up.kr_last < KCH ? P.map_col_u_part[up.kr_last / 16 - 1] : P.map_col_u;
         ce = (cudaError_t)zero_async(P.tile_ctr, sizeof(int), st);
         if (ce != cudaSuccess) return (int)ce;
         const int ntiles = (int)ceil_div(m, TILE_M);
         const int grid = ntiles < num_sms ? ntiles : num_sms;
 #define BCGS_UPD(NBT, KDT) \
         update_tc_kernel<NBT, KDT><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(                        \
-            P.map_col_u, P.map_col_u16, P.map_col_u32, P.map_col_u48, P.map_bdig##NBT, up)
+            P.map_col_u, ulast_map, P.map_bdig##NBT, up)
         if (NB == 16) {
             if (P.kd == 6) BCGS_UPD(16, 6); else BCGS_UPD(16, 7);
         } else {

@@ -47,7 +47,10 @@ constexpr int kGramSmemMax = GramPanel<32>::SMEM > GramPanel<8>::SMEM
 
 // The tile at C rows ia0.., C columns jb0.., rows [r_begin, r_end) of X, written to
 // `out` (na x nb, ld na). 256 threads; sm holds GramPanel<TB>::SMEM doubles.
-template <int TB>
+// SEG > 0: every SEG sub-tiles of GR rows the running sums are added to a total
+// and restarted, so no FMA chain is longer than SEG * GR rows however long the
+// row range is (SEG = 0: one chain over the range).
+template <int TB, int SEG = 0>
 __device__ __forceinline__ void gram_partial_body(const double* __restrict__ X, i64 ld, int a0, int na, int b0,
                                                   int nb, i64 r_begin, i64 r_end, int ia0, int jb0,
                                                   double* __restrict__ out, double* __restrict__ sm) {
@@ -59,11 +62,21 @@ __device__ __forceinline__ void gram_partial_body(const double* __restrict__ X, 
     const int ti = tid % TI;
     const int tj = tid / TI;        // TB/2 threads along C cols -> 2 cols each
 
-    double acc[4][2];
+    double acc[4][2], tot[4][2];
 #pragma unroll
-    for (int a = 0; a < 4; ++a) { acc[a][0] = 0.0; acc[a][1] = 0.0; }
+    for (int a = 0; a < 4; ++a) { acc[a][0] = 0.0; acc[a][1] = 0.0; tot[a][0] = 0.0; tot[a][1] = 0.0; }
 
+    int sub = 0;
     for (i64 r0 = r_begin; r0 < r_end; r0 += GR) {
+        if (SEG > 0 && sub == SEG) {
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                tot[a][0] += acc[a][0]; tot[a][1] += acc[a][1];
+                acc[a][0] = 0.0; acc[a][1] = 0.0;
+            }
+            sub = 0;
+        }
+        ++sub;
         // Stage A[r0:r0+GR, ia0:ia0+GA] and B[r0:r0+GR, jb0:jb0+TB]. Consecutive
         // threads read consecutive rows of one column.
         for (int e = tid; e < GR * GA; e += NT) {
@@ -94,6 +107,10 @@ __device__ __forceinline__ void gram_partial_body(const double* __restrict__ X, 
         }
         __syncthreads();
     }
+    if (SEG > 0) {
+#pragma unroll
+        for (int a = 0; a < 4; ++a) { acc[a][0] += tot[a][0]; acc[a][1] += tot[a][1]; }
+    }
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         int i = ia0 + ti + TI * a;
@@ -114,6 +131,19 @@ gram_fp64_partial(const double* __restrict__ X, i64 ld, i64 m, int a0, int na, i
     const i64 r_end = min(m, r_begin + rows_per_chunk);
     gram_partial_body<GT_B>(X, ld, a0, na, b0, nb, r_begin, r_end, blockIdx.y * GT_A, blockIdx.z * GT_B,
                             part + (i64)chunk * na * nb, sm);
+}
+
+// The same over chunks of rows_per_chunk rows, each summed in segments of
+// 256 rows (the row-sharded path's long chunks).
+__global__ void __launch_bounds__(GT_THREADS, 4)
+gram_fp64_partial_seg(const double* __restrict__ X, i64 ld, i64 m, int a0, int na, int b0, int nb,
+                      i64 rows_per_chunk, double* __restrict__ part) {
+    __shared__ double sm[GramPanel<GT_B>::SMEM];
+    const int chunk = blockIdx.x;
+    const i64 r_begin = (i64)chunk * rows_per_chunk;
+    const i64 r_end = min(m, r_begin + rows_per_chunk);
+    gram_partial_body<GT_B, 256 / GramPanel<GT_B>::GR>(X, ld, a0, na, b0, nb, r_begin, r_end, blockIdx.y * GT_A,
+                                                        blockIdx.z * GT_B, part + (i64)chunk * na * nb, sm);
 }
 
 // Fixed-order sum over chunks: out[i + j*ldo] = sum_{c=0}^{nchunks-1} part[c][i + j*na].
@@ -172,7 +202,7 @@ int launch_gram_partials_fp64(const double* X, i64 ld, i64 m, int a0, int na, in
     if (rows <= 0 || rows % GT_R != 0) return (int)cudaErrorInvalidValue;
     const i64 nchunks = ceil_div(m, rows);
     dim3 grid((unsigned)nchunks, (unsigned)ceil_div(na, GT_A), (unsigned)ceil_div(nb, GT_B));
-    gram_fp64_partial<<<grid, GT_THREADS, 0, st>>>(X, ld, m, a0, na, b0, nb, rows, part);
+    gram_fp64_partial_seg<<<grid, GT_THREADS, 0, st>>>(X, ld, m, a0, na, b0, nb, rows, part);
     g_launch_count += 1;
     return (int)cudaGetLastError();
 }
