@@ -9,11 +9,15 @@
 # orth.c includes "../tpetra/include/Tsqr.hpp"; with -I ref_stubs/include that
 # path resolves to ref_stubs/tpetra/include/Tsqr.hpp.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT   (or set BCGS_REFERENCE_ROOT)
 # Does nothing (exit 0) when the reference sources are absent.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${BCGS_REFERENCE_ROOT:-}}"
+if [ -z "$REF" ]; then
+    echo "build_ref: give the reference's root as an argument or in BCGS_REFERENCE_ROOT; skipping" >&2
+    exit 0
+fi
 OUT="$HERE/_ref"
 if [ ! -f "$REF/SRC/orth.c" ] || [ ! -f "$REF/SRC/util.c" ]; then
     echo "build_ref: reference sources not found under $REF; skipping" >&2
