@@ -80,6 +80,10 @@ struct TsqrApplyJob {
     i64 ldp;
 };
 
+// Sets the batched tile kernel's shared-memory limit on the current device
+// (outside any stream capture).
+int tsqr_tile_batched_prepare();
+
 // Launchers (items = prefix[njobs] CTAs).
 int gram_batched_panel_rows(int tb);   // A-panel height for a B-panel width
 int launch_gram_partial_batched(const GramJob* jobs, const int* prefix, int njobs, int items, cudaStream_t st);

@@ -36,6 +36,7 @@
 // and share each B tile through L2 (B loaded evict_last, A evict_first). No load
 // is multicast. Every wait is bounded; a timeout sets an
 // error word and the kernel winds down.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -44,6 +45,8 @@
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
+#include "../../include/orth_gb300.h"
+#include "batched.h"
 #include "common.cuh"
 #include "kernels.h"
 #include "split.h"
@@ -111,11 +114,11 @@ __device__ __forceinline__ unsigned short bf16_bits_of_int(int d) {
     return (unsigned short)(__float_as_uint(f) >> 16);
 }
 
-// Column max |x| (bit patterns of non-negative doubles order like the values).
-__global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c0,
-                              unsigned long long* __restrict__ cmax) {
-    const int c = c0 + blockIdx.y;
-    const i64 r0 = (i64)blockIdx.x * 4096;
+// Column max |x| (bit patterns of non-negative doubles order like the values):
+// rows [4096 rb, 4096 (rb + 1)) of column c into cmax[c].
+__device__ __forceinline__ void colmax_body(const double* __restrict__ X, i64 ld, i64 m, int c, int rb,
+                                            unsigned long long* __restrict__ cmax) {
+    const i64 r0 = (i64)rb * 4096;
     const i64 r1 = min(m, r0 + 4096);
     unsigned long long v = 0;
     for (i64 r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
@@ -138,6 +141,11 @@ __global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c
     }
 }
 
+__global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c0,
+                              unsigned long long* __restrict__ cmax) {
+    colmax_body(X, ld, m, c0 + (int)blockIdx.y, (int)blockIdx.x, cmax);
+}
+
 // Slice columns [c0, c0+nc) of X into the digit store. A CTA handles 128 rows x
 // 16 columns (grid: row tiles x column groups), one row per thread: 16 coalesced
 // column loads and the digits, staged in shared memory as [plane][64-row
@@ -146,17 +154,16 @@ __global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c
 // HBM. A full tile leaves as 2 KD bulk copies of 2 KB, issued by as many threads.
 // Ragged tiles (rows past m, or fewer than 16 columns) are stored element-wise.
 template <int KD>
-__global__ void __launch_bounds__(128, 6)
-slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
-             const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
-             unsigned short* __restrict__ colstore, i64 nrc) {
+__device__ __forceinline__ void slice_body(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
+                                           const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
+                                           unsigned short* __restrict__ colstore, i64 nrc, int bx, int by) {
     constexpr int CG = 16;                   // columns per CTA
     __shared__ __align__(128) unsigned short sdig[KD][2][CG][64];
     const int t = threadIdx.x;
-    const int g = blockIdx.y * CG;           // first column of this group (relative to c0)
-    const i64 r0 = (i64)blockIdx.x * 128;
+    const int g = by * CG;                   // first column of this group (relative to c0)
+    const i64 r0 = (i64)bx * 128;
     const i64 r = r0 + t;
-    if (blockIdx.x == 0 && t < CG && g + t < nc) cexp[c0 + g + t] = scale_exp(cmax[c0 + g + t]);
+    if (bx == 0 && t < CG && g + t < nc) cexp[c0 + g + t] = scale_exp(cmax[c0 + g + t]);
     double x[CG];
 #pragma unroll
     for (int j = 0; j < CG; ++j) x[j] = (g + j < nc && r < m) ? X[r + (i64)(c0 + g + j) * ld] : 0.0;
@@ -195,14 +202,22 @@ slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
     }
 }
 
+template <int KD>
+__global__ void __launch_bounds__(128, 6)
+slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
+             const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
+             unsigned short* __restrict__ colstore, i64 nrc) {
+    slice_body<KD>(X, ld, m, n, c0, nc, cmax, cexp, colstore, nrc, (int)blockIdx.x, (int)blockIdx.y);
+}
+
 // Right-hand factor of the update, scaled: Bp[c + j*ldb] for c < K + nc, j < nc:
 //   c <  K : -(S T^{-1})[c, j] * 2^{cexp[c]}      (or -S[c, j] * 2^{cexp[c]} if T is null)
 //   c >= K :  T^{-1}[c-K, j]   * 2^{cexp[c]}      (or the identity)
 // and the per-column max |Bp| into bmax (bit patterns).
-__global__ void __launch_bounds__(256)
-bbuild_kernel(const double* __restrict__ S, int lds, const double* __restrict__ T, int ldt, int K, int nc,
-              const int* __restrict__ cexp, double* __restrict__ Bp, int ldb,
-              unsigned long long* __restrict__ bmax) {
+__device__ __forceinline__ void bbuild_body(const double* __restrict__ S, int lds, const double* __restrict__ T,
+                                            int ldt, int K, int nc, const int* __restrict__ cexp,
+                                            double* __restrict__ Bp, int ldb, unsigned long long* __restrict__ bmax,
+                                            int bx) {
     __shared__ double ti[64][65];
     const int tid = threadIdx.x;
     // T^{-1} (upper, nc x nc, nc <= 64): column j solves T y = e_j by back substitution.
@@ -219,7 +234,7 @@ bbuild_kernel(const double* __restrict__ S, int lds, const double* __restrict__ 
         for (int e = tid; e < 64 * 64; e += blockDim.x) ti[e / 64][e % 64] = (e / 64 == e % 64) ? 1.0 : 0.0;
     }
     __syncthreads();
-    const int c = blockIdx.x * 64 + (tid & 63);
+    const int c = bx * 64 + (tid & 63);
     for (int j = tid >> 6; j < nc; j += 4) {
         double v = 0.0;
         if (c < K) {
@@ -241,6 +256,13 @@ bbuild_kernel(const double* __restrict__ S, int lds, const double* __restrict__ 
     }
 }
 
+__global__ void __launch_bounds__(256)
+bbuild_kernel(const double* __restrict__ S, int lds, const double* __restrict__ T, int ldt, int K, int nc,
+              const int* __restrict__ cexp, double* __restrict__ Bp, int ldb,
+              unsigned long long* __restrict__ bmax) {
+    bbuild_body(S, lds, T, ldt, K, nc, cexp, Bp, ldb, bmax, (int)blockIdx.x);
+}
+
 // Right-hand factor of the fused update of the lagged one-sync variants. With
 // Q = X[:, 0:K], U_k = X[:, K:K+s], X_{k+1} = X[:, K+s:K+s+nz] it produces, in one
 // product over those K + s + nz columns,
@@ -253,15 +275,15 @@ bbuild_kernel(const double* __restrict__ S, int lds, const double* __restrict__ 
 // (Y = G[0:K, 0:s], S' = [S'_top; S'_mid] of K + s rows; W = I when Ts is null, the
 // unscaled first pass of bcgsi21s). Rows are scaled by 2^cexp[c]; bmax collects
 // the column maxima.
-__global__ void __launch_bounds__(256)
-bbuild_fused_kernel(const double* __restrict__ G, int ldg, int K, int s, const double* __restrict__ Ty,
-                    int ldty, const double* __restrict__ Sp, int ldsp, const double* __restrict__ Ts,
-                    int ldts, int nz, const int* __restrict__ cexp, double* __restrict__ Bp, int ldb,
-                    unsigned long long* __restrict__ bmax) {
-    // Ty^{-1} (s x s), Ts^{-1} (nz x nz) and M (s x nz) in dynamic shared memory,
+__device__ __forceinline__ void bbuild_fused_body(const double* __restrict__ G, int ldg, int K, int s,
+                                                  const double* __restrict__ Ty, int ldty,
+                                                  const double* __restrict__ Sp, int ldsp,
+                                                  const double* __restrict__ Ts, int ldts, int nz,
+                                                  const int* __restrict__ cexp, double* __restrict__ Bp, int ldb,
+                                                  unsigned long long* __restrict__ bmax, int bx, double* fsm) {
+    // Ty^{-1} (s x s), Ts^{-1} (nz x nz) and M (s x nz) in shared memory (fsm),
     // row stride FW = 65 (s, nz <= 64).
     constexpr int FW = 65;
-    extern __shared__ double fsm[];
     double* w1 = fsm;
     double* w2 = fsm + 64 * FW;
     double* mm = fsm + 2 * 64 * FW;
@@ -299,7 +321,7 @@ bbuild_fused_kernel(const double* __restrict__ G, int ldg, int K, int s, const d
     }
     __syncthreads();
     const int kin = K + s + nz, nout = s + nz;
-    const int c = blockIdx.x * 64 + (tid & 63);
+    const int c = bx * 64 + (tid & 63);
     if (c >= kin) return;
     for (int j = tid >> 6; j < nout; j += 4) {
         double v = 0.0;
@@ -331,6 +353,15 @@ bbuild_fused_kernel(const double* __restrict__ G, int ldg, int K, int s, const d
     }
 }
 
+__global__ void __launch_bounds__(256)
+bbuild_fused_kernel(const double* __restrict__ G, int ldg, int K, int s, const double* __restrict__ Ty,
+                    int ldty, const double* __restrict__ Sp, int ldsp, const double* __restrict__ Ts,
+                    int ldts, int nz, const int* __restrict__ cexp, double* __restrict__ Bp, int ldb,
+                    unsigned long long* __restrict__ bmax) {
+    extern __shared__ double fsm[];
+    bbuild_fused_body(G, ldg, K, s, Ty, ldty, Sp, ldsp, Ts, ldts, nz, cexp, Bp, ldb, bmax, (int)blockIdx.x, fsm);
+}
+
 #undef W1
 #undef W2
 #undef MM
@@ -338,12 +369,11 @@ bbuild_fused_kernel(const double* __restrict__ G, int ldg, int K, int s, const d
 // Digits of the right-hand factor: bdig[plane][j][c] (K-major), zero padded to
 // (NB rows, Kpad columns); fexp[j] = its column scale exponent.
 template <int KD>
-__global__ void __launch_bounds__(256)
-bdigit_kernel(const double* __restrict__ Bp, int ldb, int K, int nc, int NB, int Kpad,
-              const unsigned long long* __restrict__ bmax, int* __restrict__ fexp,
-              unsigned short* __restrict__ bdig) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (blockIdx.x == 0 && threadIdx.x < NB) fexp[threadIdx.x] = threadIdx.x < nc ? scale_exp(bmax[threadIdx.x]) : 0;
+__device__ __forceinline__ void bdigit_body(const double* __restrict__ Bp, int ldb, int K, int nc, int NB, int Kpad,
+                                            const unsigned long long* __restrict__ bmax, int* __restrict__ fexp,
+                                            unsigned short* __restrict__ bdig, int bx) {
+    const int c = bx * blockDim.x + threadIdx.x;
+    if (bx == 0 && threadIdx.x < NB) fexp[threadIdx.x] = threadIdx.x < nc ? scale_exp(bmax[threadIdx.x]) : 0;
     if (c >= Kpad) return;
     for (int j = 0; j < NB; ++j) {
         int d[KD];
@@ -356,6 +386,14 @@ bdigit_kernel(const double* __restrict__ Bp, int ldb, int K, int nc, int NB, int
 #pragma unroll
         for (int i = 0; i < KD; ++i) bdig[((i64)i * NB + j) * Kpad + c] = bf16_bits_of_int(d[i]);
     }
+}
+
+template <int KD>
+__global__ void __launch_bounds__(256)
+bdigit_kernel(const double* __restrict__ Bp, int ldb, int K, int nc, int NB, int Kpad,
+              const unsigned long long* __restrict__ bmax, int* __restrict__ fexp,
+              unsigned short* __restrict__ bdig) {
+    bdigit_body<KD>(Bp, ldb, K, nc, NB, Kpad, bmax, fexp, bdig, (int)blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -569,10 +607,20 @@ struct GramParams {
     int* err;
 };
 
-template <int KD>
+// One Gram of a batched launch: its tensor maps (in global memory) and parameters.
+struct SplitGramJob {   // the CUtensorMap members keep the struct 64-byte aligned
+    CUtensorMap mapA, mapAlast, mapB;
+    GramParams p;
+};
+
+// BATCH: the CTAs of many Grams in one launch; CTA b runs item b - prefix[j] of
+// job j (prefix[j] <= b < prefix[j + 1]) with job j's maps and parameters, and
+// exactly the arithmetic of a single launch of that Gram. p0.err is the launch's.
+template <int KD, bool BATCH>
 __global__ void __launch_bounds__(NTHREADS, 1)
 gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapAlast,
-               const __grid_constant__ CUtensorMap mapB, GramParams p) {
+               const __grid_constant__ CUtensorMap mapB, GramParams p0, const SplitGramJob* __restrict__ jobs,
+               const int* __restrict__ prefix, int njobs) {
     constexpr int NB = 32;
     using L = SmemLayout<NB, KD>;
     extern __shared__ uint8_t smem_raw[];
@@ -584,7 +632,21 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     const uint32_t tmem = tmem_slot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    const int item = blockIdx.x;
+    int item = blockIdx.x;
+    GramParams p = p0;
+    const CUtensorMap *mA = &mapA, *mAl = &mapAlast, *mB = &mapB;
+    if constexpr (BATCH) {
+        const int j = batched_job_of(prefix, njobs, item);
+        item -= prefix[j];
+        p = jobs[j].p;
+        p.err = p0.err;
+        mA = &jobs[j].mapA; mAl = &jobs[j].mapAlast; mB = &jobs[j].mapB;
+        if (threadIdx.x == 0) {   // the producer: maps written by the host before the launch
+            tc::fence_tensormap(mA);
+            tc::fence_tensormap(mAl);
+            tc::fence_tensormap(mB);
+        }
+    }
     const int mb = item % p.numMB;
     const int ng = (item / p.numMB) % p.numNG;
     const int rcI = item / (p.numMB * p.numNG);
@@ -602,7 +664,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
         const int rc = (int)((r0 + (i64)ch * KCH) / KCH);   // 64-row chunk of the column store
         ax = 0; ay = mb * TILE_M; az = rc; azs = p.nrc;
         bx = 0; by = p.b0 + ng * NB; bz = rc; bzs = p.nrc;
-        amap = last_part ? &mapAlast : &mapA;
+        amap = last_part ? mAl : mA;
         abytes = last_part ? (uint32_t)(p.alast * KCH * 2) : (uint32_t)A_SLOT;
     };
 
@@ -614,7 +676,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
             const uint64_t polB = tc::policy_evict_last();
             Ring ra, rb;
             for (int ch = 0; ch < nchunks; ++ch)
-                if (!produce_chunk<NB, KD>(&mapB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag, p.err, polA,
+                if (!produce_chunk<NB, KD>(mB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag, p.err, polA,
                                            polB))
                     break;
             if (abort_flag) {
@@ -703,10 +765,24 @@ struct UpdateParams {
     int kr_last;                // columns the last K chunk's A box holds: kin - 64 (chunks - 1) rounded up to 16
 };
 
-template <int NB, int KD>
+// One update of a batched launch: its tensor maps (in global memory) and
+// parameters (tile_ctr and err are the launch's).
+struct SplitUpdJob {    // the CUtensorMap members keep the struct 64-byte aligned
+    CUtensorMap mapA, mapAlast, mapB;
+    UpdateParams p;
+};
+
+// BATCH: the row tiles of many updates in one persistent launch. Global tile t
+// belongs to job j (tprefix[j] <= t < tprefix[j + 1]) as its tile t - tprefix[j];
+// every role resolves each tile to its job, and each tile gets exactly the
+// arithmetic of a single launch of that update. A CTA takes tiles in increasing
+// order, so its jobs come in increasing order too; the epilogue writes a job's
+// column maxima when the next job starts.
+template <int NB, int KD, bool BATCH>
 __global__ void __launch_bounds__(NTHREADS, 1)
 update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapAlast,
-                 const __grid_constant__ CUtensorMap mapB, UpdateParams p) {
+                 const __grid_constant__ CUtensorMap mapB, UpdateParams p0, const SplitUpdJob* __restrict__ jobs,
+                 const int* __restrict__ tprefix, int njobs) {
     using L = SmemLayout<NB, KD>;
     extern __shared__ uint8_t smem_raw[];
     __shared__ uint32_t tmem_slot;
@@ -717,31 +793,31 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     const uint32_t tmem = tmem_slot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    const int ntiles = (int)ceil_div(p.m, TILE_M);
-    const int nchunks = (p.kin + KCH - 1) / KCH;
-    const int nwin = (nchunks + WIN - 1) / WIN;
+    const int ntiles = BATCH ? tprefix[njobs] : (int)ceil_div(p0.m, TILE_M);
     __shared__ unsigned long long s_cmax[32];
     if (threadIdx.x < 32) s_cmax[threadIdx.x] = 0ULL;
     __syncthreads();
 
-    // The last K chunk loads only its kv = kin - ch * KCH columns, rounded up to 16
-    // (a box of kv columns x two 64-row chunks; the second chunk lands kv * 128
-    // bytes after the first), and issues only their MMA K steps.
-    const int kr_last = p.kr_last;   // 16, 32, 48 (mapAlast's box) or 64
-    auto coords = [&](int tile, int ch, int& ax, int& ay, int& az, int& azs, int& bx, int& by, int& bz, int& bzs,
-                      const CUtensorMap*& amap, uint32_t& abytes) {
-        ax = 0; ay = ch * KCH; az = 2 * tile; azs = p.nrc;   // 64 columns x two 64-row chunks
-        bx = ch * KCH; by = 0; bz = 0; bzs = 1;
-        const bool last = ch == nchunks - 1 && kr_last < KCH;
-        amap = last ? &mapAlast : &mapA;
-        abytes = (uint32_t)((last ? kr_last : KCH) * 256);
+    // Tile t -> its job's parameters and its tile index within the job.
+    auto resolve = [&](int t, int& lt, int& job) -> const UpdateParams* {
+        if constexpr (BATCH) {
+            job = batched_job_of(tprefix, njobs, t);
+            lt = t - tprefix[job];
+            return &jobs[job].p;
+        } else {
+            job = 0;
+            lt = t;
+            return &p0;
+        }
     };
 
     // Row tiles are handed out dynamically: the producer takes the next tile number
     // from the launch's counter and publishes it through the ring s_tile/q_*; the
     // MMA thread and every epilogue warp read the same sequence. A number >= ntiles
     // ends all three loops. Each tile's arithmetic does not depend on which CTA
-    // runs it.
+    // runs it. The last K chunk loads only its kv = kin - ch * KCH columns, rounded
+    // up to 16 (a box of kv columns x two 64-row chunks; the second chunk lands
+    // kv * 128 bytes after the first), and issues only their MMA K steps.
     __shared__ int s_tile[RQ];
     if (warp == 0) {
         if (lane == 0) {
@@ -750,16 +826,40 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
             const uint64_t polB = tc::policy_evict_last();
             Ring ra, rb, rq;
             bool ok = true;
+            int fenced = -1;
             while (ok) {
-                const int tile = atomicAdd(p.tile_ctr, 1);
-                if (!tc::mbar_wait(&bars->q_empty[rq.slot], rq.phase ^ 1u, &abort_flag, p.err, 15)) break;
+                const int tile = atomicAdd(p0.tile_ctr, 1);
+                if (!tc::mbar_wait(&bars->q_empty[rq.slot], rq.phase ^ 1u, &abort_flag, p0.err, 15)) break;
                 s_tile[rq.slot] = tile;
                 tc::mbar_arrive(&bars->q_full[rq.slot]);
                 rq.advance(RQ);
                 if (tile >= ntiles) break;
+                int lt, job;
+                const UpdateParams* q = resolve(tile, lt, job);
+                const CUtensorMap *mA = &mapA, *mAl = &mapAlast, *mB = &mapB;
+                if constexpr (BATCH) {
+                    mA = &jobs[job].mapA; mAl = &jobs[job].mapAlast; mB = &jobs[job].mapB;
+                    if (job != fenced) {   // maps written by the host before the launch
+                        tc::fence_tensormap(mA);
+                        tc::fence_tensormap(mAl);
+                        tc::fence_tensormap(mB);
+                        fenced = job;
+                    }
+                }
+                const int nchunks = (q->kin + KCH - 1) / KCH;
+                const int kr_last = q->kr_last;   // 16, 32, 48 (mapAlast's box) or 64
+                const int nrc = q->nrc;
+                auto coords = [&](int tl, int ch, int& ax, int& ay, int& az, int& azs, int& bx, int& by, int& bz,
+                                  int& bzs, const CUtensorMap*& amap, uint32_t& abytes) {
+                    ax = 0; ay = ch * KCH; az = 2 * tl; azs = nrc;   // 64 columns x two 64-row chunks
+                    bx = ch * KCH; by = 0; bz = 0; bzs = 1;
+                    const bool last = ch == nchunks - 1 && kr_last < KCH;
+                    amap = last ? mAl : mA;
+                    abytes = (uint32_t)((last ? kr_last : KCH) * 256);
+                };
                 for (int ch = 0; ch < nchunks && ok; ++ch)
-                    ok = produce_chunk<NB, KD>(&mapB, sA, sB, bars, ra, rb, coords, tile, ch, &abort_flag, p.err,
-                                               polA, polB);
+                    ok = produce_chunk<NB, KD>(mB, sA, sB, bars, ra, rb, coords, lt, ch, &abort_flag, p0.err, polA,
+                                               polB);
             }
             if (abort_flag) {
                 drain_ring(bars->a_full, RA, ra);
@@ -772,21 +872,26 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
             bool ok = true;
             int wc = 0;  // window counter across tiles
             while (ok) {
-                if (!tc::mbar_wait(&bars->q_full[rq.slot], rq.phase, &abort_flag, p.err, 33)) break;
+                if (!tc::mbar_wait(&bars->q_full[rq.slot], rq.phase, &abort_flag, p0.err, 33)) break;
                 const int tile = s_tile[rq.slot];
                 tc::mbar_arrive(&bars->q_empty[rq.slot]);
                 rq.advance(RQ);
                 if (tile >= ntiles) break;
+                int lt, job;
+                const UpdateParams* q = resolve(tile, lt, job);
+                const int nchunks = (q->kin + KCH - 1) / KCH;
+                const int nwin = (nchunks + WIN - 1) / WIN;
+                const int kr_last = q->kr_last;
                 for (int w = 0; w < nwin && ok; ++w, ++wc) {
                     const int buf = wc & 1;
                     const uint32_t tph = (uint32_t)((wc >> 1) & 1);
-                    if (!tc::mbar_wait(&bars->t_empty[buf], tph ^ 1u, &abort_flag, p.err, 32)) { ok = false; break; }
+                    if (!tc::mbar_wait(&bars->t_empty[buf], tph ^ 1u, &abort_flag, p0.err, 32)) { ok = false; break; }
                     tc::tc_fence_after();
                     const int c_end = min(nchunks, (w + 1) * WIN);
                     for (int ch = w * WIN; ch < c_end && ok; ++ch) {
                         const int kr = ch == nchunks - 1 ? kr_last : KCH;
                         ok = mma_chunk<NB, KD, true>(tmem, (uint32_t)(buf * L::TMEM_COLS_PER_BUF), sA, sB, bars, ra,
-                                                     rb, ch == w * WIN, &abort_flag, p.err, kr / 16,
+                                                     rb, ch == w * WIN, &abort_flag, p0.err, kr / 16,
                                                      (uint32_t)(kr * 128));
                     }
                     if (ok) tc::mma_commit(&bars->t_full[buf]);
@@ -804,14 +909,30 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
         Ring rq;
         // Running max over this thread's rows of the high word of |x| per output
         // column: the digit scale needs only the exponent of the column max, which
-        // the high word holds. Reduced over the CTA once, after the last tile.
+        // the high word holds. Reduced over the CTA once, after the last tile (or,
+        // in a batched launch, when the job changes).
         uint32_t rmax[NH];
 #pragma unroll
         for (int jj = 0; jj < NH; ++jj) rmax[jj] = 0u;
+        const UpdateParams* cq = nullptr;   // the job rmax belongs to (batched launches)
+        auto flush = [&](const UpdateParams* fq) {
+#pragma unroll
+            for (int jj = 0; jj < NH; ++jj) {
+                uint32_t a = rmax[jj];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const uint32_t b = __shfl_xor_sync(0xffffffffu, a, o);
+                    a = a > b ? a : b;
+                }
+                const int j = half * NH + jj;
+                if (lane == 0 && a && j < fq->nc) atomicMax(fq->cmax + fq->c0 + j, (unsigned long long)a << 32);
+                rmax[jj] = 0u;
+            }
+        };
         while (ok) {
             int tile = 0;
             if (lane == 0) {
-                if (!tc::mbar_wait(&bars->q_full[rq.slot], rq.phase, &abort_flag, p.err, 43)) tile = -1;
+                if (!tc::mbar_wait(&bars->q_full[rq.slot], rq.phase, &abort_flag, p0.err, 43)) tile = -1;
                 else tile = s_tile[rq.slot];
             }
             tile = __shfl_sync(0xffffffffu, tile, 0);
@@ -820,6 +941,16 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
             if (lane == 0) tc::mbar_arrive(&bars->q_empty[rq.slot]);
             rq.advance(RQ);
             if (tile >= ntiles) break;
+            int lt, job;
+            const UpdateParams* q = resolve(tile, lt, job);
+            if constexpr (BATCH) {
+                if (q != cq) {
+                    if (cq) flush(cq);
+                    cq = q;
+                }
+            }
+            const int nchunks = (q->kin + KCH - 1) / KCH;
+            const int nwin = (nchunks + WIN - 1) / WIN;
             long long hi[NH], mid[NH];
             float lo[NH];
 #pragma unroll
@@ -827,7 +958,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
             for (int w = 0; w < nwin; ++w, ++wc) {
                 const int buf = wc & 1;
                 const uint32_t tph = (uint32_t)((wc >> 1) & 1);
-                if (!tc::mbar_wait(&bars->t_full[buf], tph, &abort_flag, p.err, 42)) { ok = false; break; }
+                if (!tc::mbar_wait(&bars->t_full[buf], tph, &abort_flag, p0.err, 42)) { ok = false; break; }
                 tc::tc_fence_after();
                 const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * L::TMEM_COLS_PER_BUF);
                 accumulate_window<NB, KD>(taddr, half * NH, hi, mid, lo);
@@ -835,36 +966,41 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
                 tc::mbar_arrive(&bars->t_empty[buf]);
             }
             if (!ok || abort_flag) break;
-            const i64 r = (i64)tile * TILE_M + rloc;
-            double* xr = p.X + r + (i64)p.c0 * p.ld;
+            const i64 r = (i64)lt * TILE_M + rloc;
+            double* xr = q->X + r + (i64)q->c0 * q->ld;
 #pragma unroll
             for (int jj = 0; jj < NH; ++jj) {
                 const int j = half * NH + jj;
-                if (j < p.nc && r < p.m) {
-                    const double v = assemble(hi[jj], mid[jj], lo[jj], p.fexp[j] - 78);
-                    xr[(i64)j * p.ld] = v;
+                if (j < q->nc && r < q->m) {
+                    const double v = assemble(hi[jj], mid[jj], lo[jj], q->fexp[j] - 78);
+                    xr[(i64)j * q->ld] = v;
                     uint32_t a = (uint32_t)((unsigned long long)__double_as_longlong(v) >> 32) & 0x7FFFFFFFu;
                     if ((a >> 20) == 0x7FFu) a = 0u;   // Inf/NaN do not set the scale
                     rmax[jj] = a > rmax[jj] ? a : rmax[jj];
                 }
             }
         }
+        if constexpr (BATCH) {
+            if (cq) flush(cq);
+        } else {
 #pragma unroll
-        for (int jj = 0; jj < NH; ++jj) {
-            uint32_t a = rmax[jj];
+            for (int jj = 0; jj < NH; ++jj) {
+                uint32_t a = rmax[jj];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const uint32_t b = __shfl_xor_sync(0xffffffffu, a, o);
-                a = a > b ? a : b;
+                for (int o = 16; o > 0; o >>= 1) {
+                    const uint32_t b = __shfl_xor_sync(0xffffffffu, a, o);
+                    a = a > b ? a : b;
+                }
+                const int j = half * NH + jj;
+                if (lane == 0 && a && j < p0.nc) atomicMax(&s_cmax[j], (unsigned long long)a << 32);
             }
-            const int j = half * NH + jj;
-            if (lane == 0 && a && j < p.nc) atomicMax(&s_cmax[j], (unsigned long long)a << 32);
         }
     }
     __syncthreads();
-    if (threadIdx.x < p.nc && s_cmax[threadIdx.x]) atomicMax(p.cmax + p.c0 + threadIdx.x, s_cmax[threadIdx.x]);
+    if (!BATCH && threadIdx.x < p0.nc && s_cmax[threadIdx.x])
+        atomicMax(p0.cmax + p0.c0 + threadIdx.x, s_cmax[threadIdx.x]);
     if (warp == 1) {
-        if (lane == 0) tc::mbar_wait(&bars->drain, 0, &abort_flag, p.err, 52);
+        if (lane == 0) tc::mbar_wait(&bars->drain, 0, &abort_flag, p0.err, 52);
         __syncwarp();
         tc::tc_fence_after();
         tc::tmem_dealloc(tmem, (uint32_t)L::TMEM_ALLOC);
@@ -1065,12 +1201,12 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
     if (rc) return rc;
     // Shared-memory limits of the tensor-core kernels on this device.
-    rc = set_smem(gram_tc_kernel<6>, SmemLayout<32, 6>::BYTES);
-    if (!rc) rc = set_smem(gram_tc_kernel<7>, SmemLayout<32, 7>::BYTES);
-    if (!rc) rc = set_smem(update_tc_kernel<16, 6>, SmemLayout<16, 6>::BYTES);
-    if (!rc) rc = set_smem(update_tc_kernel<16, 7>, SmemLayout<16, 7>::BYTES);
-    if (!rc) rc = set_smem(update_tc_kernel<32, 6>, SmemLayout<32, 6>::BYTES);
-    if (!rc) rc = set_smem(update_tc_kernel<32, 7>, SmemLayout<32, 7>::BYTES);
+    rc = set_smem(gram_tc_kernel<6, false>, SmemLayout<32, 6>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<7, false>, SmemLayout<32, 7>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<16, 6, false>, SmemLayout<16, 6>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<16, 7, false>, SmemLayout<16, 7>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<32, 6, false>, SmemLayout<32, 6>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<32, 7, false>, SmemLayout<32, 7>::BYTES);
     return rc;
 }
 
@@ -1138,8 +1274,12 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     const CUtensorMap& alast_map = gp.alast < TILE_M ? P.map_col_a_part[gp.alast / 16 - 1] : P.map_col_a;
     const unsigned grid = (unsigned)(mbn * gp.rc);
     const int smem = P.kd == 6 ? SmemLayout<32, 6>::BYTES : SmemLayout<32, 7>::BYTES;
-    if (P.kd == 6) gram_tc_kernel<6><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp);
-    else gram_tc_kernel<7><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp);
+    if (P.kd == 6)
+        gram_tc_kernel<6, false><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp, nullptr,
+                                                               nullptr, 0);
+    else
+        gram_tc_kernel<7, false><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp, nullptr,
+                                                               nullptr, 0);
     g_launch_count += 1;
     rc = (int)cudaGetLastError();
     if (rc) return rc;
@@ -1178,8 +1318,8 @@ static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int 
         const int ntiles = (int)ceil_div(m, TILE_M);
         const int grid = ntiles < num_sms ? ntiles : num_sms;
 #define BCGS_UPD(NBT, KDT) \
-        update_tc_kernel<NBT, KDT><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(                        \
-            P.map_col_u, ulast_map, P.map_bdig##NBT, up)
+        update_tc_kernel<NBT, KDT, false><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(                 \
+            P.map_col_u, ulast_map, P.map_bdig##NBT, up, nullptr, nullptr, 0)
         if (NB == 16) {
             if (P.kd == 6) BCGS_UPD(16, 6); else BCGS_UPD(16, 7);
         } else {

@@ -118,6 +118,12 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// Makes a tensor map that the host wrote to global memory before the launch
+// visible to this thread's later TMA operations through the tensormap proxy.
+__device__ __forceinline__ void fence_tensormap(const void* map) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
+}
+
 // L2 eviction policies for TMA loads: operands streamed once are loaded
 // evict_first, operands that other CTAs read again soon (the Gram's B tiles,
 // the update's right-hand factor) evict_last, so that the re-reads hit in L2
