@@ -187,15 +187,24 @@ void orth_gb300_set_gram_chunk_rows(long long rows);
  * s[b] <= 16. flags: ORTH_GB300_BATCH_TUNE times the Gram's panel width and chunk
  * rows per block size on the batch itself (reads X, writes only the plan's
  * scratch).
- * precision ORTH_GB300_SPLIT_BF16 / _FAST: any variant, s[b] <= 64. Each run
- * spreads the matrices over up to 16 scratch slots (as many as fit in half of the
- * free device memory; longest first to the least loaded slot), each on its own
- * stream forked from and joined back into `stream`,
- * and runs them through the single-matrix tensor-core driver (no graph; a slot's
- * digit store, 14 bytes per element, is sized for its largest matrix and
- * reused). Breakdowns and split-kernel timeouts are collected per matrix on the
- * device. The slots are the library's own scratch: order any later library call
- * after the run (same stream, or a synchronize).
+ * precision ORTH_GB300_SPLIT_BF16 / _FAST:
+ *   - ORTH_GB300_BCGSI2P1S with every s[b] <= 16 (the default form): staged
+ *     graphs. The matrices are taken in order into waves whose digit stores
+ *     (14 bytes per element) and scratch fit in 85 % of the free device memory at
+ *     creation; in a wave every stage of the split driver (slicing, the
+ *     tensor-core Gram and its reduction, the small FP64 operations, the factor,
+ *     its digits, the fused update; the TSQR of block 1) is one launch over all
+ *     its matrices, and each wave is one captured CUDA graph; a run replays the
+ *     wave graphs in order on `stream`. Each matrix's Q and R are bit-identical to
+ *     orth_gb300_run_dev's in the same precision.
+ *   - any variant, s[b] <= 64 (and the flags ORTH_GB300_BATCH_STREAMS or
+ *     ORTH_GB300_BATCH_ONE_STREAM): each run spreads the matrices over up to 16
+ *     scratch slots (as many as fit in half of the free device memory; longest
+ *     first to the least loaded slot), each on its own stream forked from and
+ *     joined back into `stream`, and runs them through the single-matrix
+ *     tensor-core driver (no graph). The slots are the library's own scratch:
+ *     order any later library call after the run (same stream, or a synchronize).
+ *   Breakdowns and split-kernel timeouts are collected per matrix on the device.
  * The plan owns its device workspace; runs must not overlap.
  * Returns 0, 2 (invalid arguments), 3 (CUDA failure), 4 (variant/precision not
  * available in batched form).
@@ -204,6 +213,8 @@ typedef struct orth_gb300_batch orth_gb300_batch;
 #define ORTH_GB300_BATCH_TUNE 1
 /* Split-precision batches: use one stream and one scratch slot (less device memory). */
 #define ORTH_GB300_BATCH_ONE_STREAM 2
+/* Split-precision batches: the per-matrix driver on concurrent streams instead of staged graphs. */
+#define ORTH_GB300_BATCH_STREAMS 4
 int orth_gb300_batch_create(orth_gb300_batch **plan, int variant, int count, const int *m, const int *n,
                             const int *s, double *const *dX, const long long *ldX, double *const *dR,
                             const int *ldR, int precision, int flags, void *stream);
@@ -218,6 +229,14 @@ int orth_gb300_batch_info(const orth_gb300_batch *plan, long long *launches_per_
 void orth_gb300_batch_destroy(orth_gb300_batch *plan);
 /* The schedule without a GPU: stages, launches per run and device bytes a plan
  * for these shapes would hold. */
+/*
+ * The staged split-precision plan of a batch, without a GPU: how many waves a
+ * wave budget of budget_bytes gives, the kernel launches of one run, and the
+ * bytes of the largest wave's device buffer. 0, 2 (invalid shapes) or 4 (s > 16).
+ */
+int orth_gb300_split_batch_dry_run(int count, const int *m, const int *n, const int *s, long long budget_bytes,
+                                   int *waves, long long *launches_per_run, long long *wave_bytes);
+
 int orth_gb300_batch_dry_run(int count, const int *m, const int *n, const int *s, long long *stages,
                              long long *launches_per_run, long long *workspace_bytes);
 /* The schedule of a split-precision batch without a GPU: returns the number of

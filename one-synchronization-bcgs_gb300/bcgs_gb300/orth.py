@@ -136,6 +136,9 @@ def load(path: str | None = None):
     lib.orth_gb300_batch_destroy.restype = None
     lib.orth_gb300_batch_dry_run.argtypes = [ctypes.c_int, P_int, P_int, P_int, P_ll, P_ll, P_ll]
     lib.orth_gb300_batch_dry_run.restype = ctypes.c_int
+    lib.orth_gb300_split_batch_dry_run.argtypes = [ctypes.c_int, P_int, P_int, P_int, ctypes.c_longlong, P_int, P_ll,
+                                                   P_ll]
+    lib.orth_gb300_split_batch_dry_run.restype = ctypes.c_int
     lib.orth_gb300_split_batch_plan.argtypes = [ctypes.c_int, P_int, P_int, P_int, ctypes.c_longlong, ctypes.c_int,
                                                 P_int, P_int]
     lib.orth_gb300_split_batch_plan.restype = ctypes.c_int
@@ -383,6 +386,7 @@ def set_gram_chunk_rows(rows: int) -> None:
 
 BATCH_TUNE = 1
 BATCH_ONE_STREAM = 2
+BATCH_STREAMS = 4
 
 
 def _int_array(v):
@@ -395,6 +399,16 @@ def batch_dry_run(ms, ns, ss) -> dict:
     rc = int(load().orth_gb300_batch_dry_run(len(ms), _int_array(ms), _int_array(ns), _int_array(ss),
                                              ctypes.byref(st), ctypes.byref(la), ctypes.byref(wb)))
     return {"rc": rc, "stages": st.value, "launches": la.value, "bytes": wb.value}
+
+
+def split_batch_dry_run(ms, ns, ss, budget_bytes: int) -> dict:
+    """Waves, launches per run and wave-buffer bytes of a staged split-precision
+    batch (orth_gb300_split_batch_dry_run; no GPU needed)."""
+    w, la, by = ctypes.c_int(0), ctypes.c_longlong(0), ctypes.c_longlong(0)
+    rc = int(load().orth_gb300_split_batch_dry_run(len(ms), _int_array(ms), _int_array(ns), _int_array(ss),
+                                                   int(budget_bytes), ctypes.byref(w), ctypes.byref(la),
+                                                   ctypes.byref(by)))
+    return {"rc": rc, "waves": w.value, "launches": la.value, "bytes": by.value}
 
 
 def split_batch_plan(ms, ns, ss, free_bytes: int = -1, max_slots: int = 0) -> dict:
@@ -417,7 +431,7 @@ class Batch:
     """
 
     def __init__(self, ms, ns, ss, x_ptrs, r_ptrs, ldx=None, ldr=None, precision=FP64, tune=True,
-                 stream: int = 0, variant: str = "bcgsi2P1s", one_stream: bool = False):
+                 stream: int = 0, variant: str = "bcgsi2P1s", one_stream: bool = False, streams: bool = False):
         lib = load()
         self.count = len(ms)
         self._h = ctypes.c_void_p(0)
@@ -427,7 +441,8 @@ class Batch:
         lr = _int_array(ldr if ldr is not None else ns)
         self.rc = int(lib.orth_gb300_batch_create(ctypes.byref(self._h), VARIANT_ID[variant], self.count,
                                                   _int_array(ms), _int_array(ns), _int_array(ss), xs, lx, rs, lr,
-                                                  precision, (BATCH_TUNE if tune else 0) | (BATCH_ONE_STREAM if one_stream else 0),
+                                                  precision, (BATCH_TUNE if tune else 0) | (BATCH_ONE_STREAM if one_stream else 0)
+                                                  | (BATCH_STREAMS if streams else 0),
                                                   ctypes.c_void_p(stream)))
 
     def run(self, stream: int = 0) -> int:

@@ -32,6 +32,7 @@
 #include "batched.h"
 #include "common.cuh"
 #include "kernels.h"
+#include "split.h"
 
 namespace bcgs {
 
@@ -121,8 +122,10 @@ struct BatchPlan {
     cudaGraphExec_t exec = nullptr;
     long long launches = 0;
     int graph_nodes = 0;
-    // Split-precision batches run the single-matrix driver per matrix (no graph).
+    // Split-precision batches: staged graphs per wave (BCGSI+P-1S, s <= 16), or the
+    // single-matrix driver per matrix on concurrent streams.
     bool split = false;
+    SplitStaged* staged = nullptr;
     int variant = 0, precision = 0, max_slots = 0;
     std::vector<int> vm, vn, vs, vldR;
     std::vector<double*> vX, vR;
@@ -579,6 +582,7 @@ int autotune(BatchPlan& P, cudaStream_t st) {
 
 void free_plan(BatchPlan* P) {
     if (!P) return;
+    if (P->staged) split_staged_destroy(P->staged);
     if (P->dstatus) cudaFree(P->dstatus);
     if (P->exec) cudaGraphExecDestroy(P->exec);
     if (P->graph) cudaGraphDestroy(P->graph);
@@ -642,6 +646,18 @@ int orth_gb300_batch_create(orth_gb300_batch** out, int variant, int count, cons
             free_plan(P);
             return 3;
         }
+        if (!(flags & (ORTH_GB300_BATCH_ONE_STREAM | ORTH_GB300_BATCH_STREAMS)) &&
+            split_staged_supported(variant, count, s)) {
+            const int rc = split_staged_create(count, m, n, s, dX, ldX, dR, ldR,
+                                               precision == ORTH_GB300_SPLIT_BF16_FAST ? 6 : 7, P->dstatus, -1,
+                                               (cudaStream_t)stream, &P->staged);
+            if (rc) { free_plan(P); return rc; }
+            long long k = 0;
+            int nodes = 0;
+            split_staged_info(P->staged, &k, nullptr, &nodes, nullptr);
+            P->launches = k;
+            P->graph_nodes = nodes;
+        }
         *out = new orth_gb300_batch{P};
         return 0;
     }
@@ -681,6 +697,7 @@ int orth_gb300_batch_create(orth_gb300_batch** out, int variant, int count, cons
 int orth_gb300_batch_run(orth_gb300_batch* h, void* stream) {
     if (!h || !h->plan) return 2;
     cudaStream_t st = (cudaStream_t)stream;
+    if (h->plan->staged) return bcgs::split_staged_run(h->plan->staged, st);
     if (h->plan->split) {
         BatchPlan& P = *h->plan;
         const long long l0 = bcgs::g_launch_count;
@@ -724,6 +741,7 @@ int orth_gb300_batch_info(const orth_gb300_batch* h, long long* launches_per_run
     const BatchPlan& P = *h->plan;
     if (launches_per_run) *launches_per_run = P.launches;
     if (workspace_bytes) *workspace_bytes = (long long)(P.ws_bytes + P.jobs_bytes);
+    if (P.staged && workspace_bytes) split_staged_info(P.staged, nullptr, workspace_bytes, nullptr, nullptr);
     if (graph_nodes) *graph_nodes = P.graph_nodes;
     if (tuned)
         for (int c = 0; c < kClasses; ++c) { tuned[2 * c] = P.tb[c]; tuned[2 * c + 1] = P.rows[c]; }
@@ -734,6 +752,13 @@ void orth_gb300_batch_destroy(orth_gb300_batch* h) {
     if (!h) return;
     bcgs::free_plan(h->plan);
     delete h;
+}
+
+int orth_gb300_split_batch_dry_run(int count, const int* m, const int* n, const int* s, long long budget_bytes,
+                                   int* waves, long long* launches_per_run, long long* wave_bytes) {
+    if (count < 1 || !m || !n || !s) return 2;
+    if (!bcgs::split_staged_supported(ORTH_GB300_BCGSI2P1S, count, s)) return 4;
+    return bcgs::split_staged_dry_run(count, m, n, s, budget_bytes, waves, launches_per_run, wave_bytes);
 }
 
 int orth_gb300_batch_dry_run(int count, const int* m, const int* n, const int* s, long long* stages,

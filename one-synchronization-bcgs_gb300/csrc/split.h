@@ -50,4 +50,22 @@ int launch_fused_update_split(double* X, i64 ld, i64 m, int K, int s, int nz, co
                               const double* Ty, const double* Sp, int ldsp, const double* Ts, int num_sms,
                               cudaStream_t st);
 
+// Staged split-precision batches (BCGSI+P-1S, s <= 16): one launch per stage for
+// all matrices of a wave, each wave one captured graph (split_bf16.cu).
+struct SplitStaged;
+bool split_staged_supported(int variant, int count, const int* s);
+// kd: 7 or 6 digit planes; dstatus: 8 ints per matrix on the device (status words,
+// split error word); budget: bytes of device memory for a wave (< 0: from the free
+// memory). Returns 0, 2 (invalid shapes) or 3.
+int split_staged_create(int count, const int* m, const int* n, const int* s, double* const* dX,
+                        const long long* ldX, double* const* dR, const int* ldR, int kd, int* dstatus,
+                        long long budget, cudaStream_t st, SplitStaged** out);
+int split_staged_run(SplitStaged* plan, cudaStream_t st);
+void split_staged_destroy(SplitStaged* plan);
+void split_staged_info(const SplitStaged* plan, long long* kernels, long long* bytes, int* nodes, int* waves);
+// The same planning without a GPU: waves, kernel launches per run and the wave
+// buffer's bytes for a given budget.
+int split_staged_dry_run(int count, const int* m, const int* n, const int* s, long long budget, int* waves,
+                         long long* kernels, long long* bytes);
+
 }  // namespace bcgs

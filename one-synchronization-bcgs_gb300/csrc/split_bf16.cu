@@ -1367,4 +1367,903 @@ int launch_fused_update_split(double* X, i64 ld, i64 m, int K, int s, int nz, co
     return finish_update(X, ld, m, kin, K, nout, num_sms, st);
 }
 
+// ===========================================================================
+// Staged split-precision batches: many independent BCGSI+P-1S QRs (the
+// reference's bcgsi2P1s, SRC/orth.c:48-222, on each matrix) in the split form,
+// with one launch per stage for all matrices of a wave.
+//
+// A wave is a set of matrices whose digit stores (14 bytes per element) and
+// scratch fit in the plan's device buffer together. For every matrix the planner
+// replays the single-matrix split driver's schedule (the TSQR of block 1, then per
+// block step: slicing of stale columns, the tensor-core Gram and its fixed-order
+// reduction, the small FP64 operations, the right-hand factor, its digits and the
+// fused tensor-core update), recording each primitive's parameters exactly as the
+// single-matrix launchers compute them (row ranges, chunk counts, digit freshness,
+// scales). Every phase then becomes one batched launch over all matrices that have
+// it, and each wave is captured as one CUDA graph. Each matrix gets the arithmetic
+// of a single run: results are bit-identical to orth_gb300_run_dev in split mode.
+// ===========================================================================
+namespace {
+
+struct ColmaxJob {
+    const double* X;
+    i64 ld, m;
+    int c0, nrb;
+    unsigned long long* cmax;
+};
+struct SliceJob {
+    const double* X;
+    i64 ld, m, nrc;
+    int n, c0, nc, ntile;
+    const unsigned long long* cmax;
+    int* cexp;
+    unsigned short* colstore;
+};
+struct BbuildJob {
+    int fused;
+    const double *S, *T, *G, *Ty, *Sp, *Ts;
+    int lds, ldt, ldg, ldsp, K, nc, s, nz;
+    const int* cexp;
+    double* Bp;
+    int ldb;
+    unsigned long long* bmax;
+};
+struct BdigitJob {
+    const double* Bp;
+    int ldb, K, nc, NB, Kpad;
+    const unsigned long long* bmax;
+    int* fexp;
+    unsigned short* bdig;
+};
+struct ZeroJob {
+    void* p;
+    int bytes;
+};
+
+__global__ void __launch_bounds__(256)
+colmax_batched(const ColmaxJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
+    const int j = batched_job_of(prefix, njobs, blockIdx.x);
+    const ColmaxJob& J = jobs[j];
+    const int it = blockIdx.x - prefix[j];
+    colmax_body(J.X, J.ld, J.m, J.c0 + it / J.nrb, it % J.nrb, J.cmax);
+}
+
+template <int KD>
+__global__ void __launch_bounds__(128, 6)
+slice_batched(const SliceJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
+    const int j = batched_job_of(prefix, njobs, blockIdx.x);
+    const SliceJob& J = jobs[j];
+    const int it = blockIdx.x - prefix[j];
+    slice_body<KD>(J.X, J.ld, J.m, J.n, J.c0, J.nc, J.cmax, J.cexp, J.colstore, J.nrc, it % J.ntile, it / J.ntile);
+}
+
+__global__ void __launch_bounds__(256)
+bbuild_batched(const BbuildJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
+    extern __shared__ double fsm[];
+    const int j = batched_job_of(prefix, njobs, blockIdx.x);
+    const BbuildJob& J = jobs[j];
+    const int it = blockIdx.x - prefix[j];
+    if (J.fused)
+        bbuild_fused_body(J.G, J.ldg, J.K, J.s, J.Ty, J.s, J.Sp, J.ldsp, J.Ts, J.nz, J.nz, J.cexp, J.Bp, J.ldb,
+                          J.bmax, it, fsm);
+    else
+        bbuild_body(J.S, J.lds, J.T, J.ldt, J.K, J.nc, J.cexp, J.Bp, J.ldb, J.bmax, it);
+}
+
+template <int KD>
+__global__ void __launch_bounds__(256)
+bdigit_batched(const BdigitJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
+    const int j = batched_job_of(prefix, njobs, blockIdx.x);
+    const BdigitJob& J = jobs[j];
+    bdigit_body<KD>(J.Bp, J.ldb, J.K, J.nc, J.NB, J.Kpad, J.bmax, J.fexp, J.bdig, blockIdx.x - prefix[j]);
+}
+
+__global__ void __launch_bounds__(256) zero_list(const ZeroJob* __restrict__ jobs) {
+    const ZeroJob& J = jobs[blockIdx.x];
+    unsigned char* p = static_cast<unsigned char*>(J.p);
+    for (int i = threadIdx.x; i < J.bytes; i += blockDim.x) p[i] = 0;
+}
+
+// Copies the batch's error word into every matrix's status slot [4].
+__global__ void spread_error(const int* __restrict__ err, int* __restrict__ dstatus, int count) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < count) dstatus[8 * (i64)b + 4] = *err;
+}
+
+constexpr size_t kBbuildSmem = 3 * 64 * 65 * sizeof(double);
+
+enum SKind {
+    kSZero, kSColmax, kSSlice, kSGram, kSReduce, kSSmall, kSBbuild, kSBdigit, kSUpdate, kSTile, kSRoot, kSApply,
+    kSZeroBuf
+};
+struct SLaunch {
+    int kind;
+    size_t job_off, prefix_off;
+    int njobs, items;
+    i64 bytes;   // kSZeroBuf
+};
+
+struct SBlob {
+    std::vector<char> bytes;
+    template <class T>
+    size_t put(const std::vector<T>& v) {
+        size_t off = (bytes.size() + 127) & ~(size_t)127;
+        bytes.resize(off + v.size() * sizeof(T));
+        if (!v.empty()) std::memcpy(bytes.data() + off, v.data(), v.size() * sizeof(T));
+        return off;
+    }
+};
+
+// One matrix of a staged batch.
+struct SMat {
+    int b;
+    i64 m, ld;
+    int n, s, p;
+    double* X;
+    double* R;
+    int ldR;
+    int* status;
+    size_t off = 0, bytes = 0;   // its region of the wave buffer
+    Plan P;                      // digit store, maps and freshness (as a single run's)
+    double *G1 = nullptr, *G2 = nullptr, *Scol = nullptr, *Sd = nullptr, *Yd = nullptr, *tsqr = nullptr;
+};
+
+i64 smat_small_doubles(int n, int s) { return 2LL * (n + s) * 2 * s + (i64)n * s + 3LL * s * s + 64; }
+
+// Bytes of one matrix's region of the wave buffer (digit store, factor, Gram
+// partials, FP64 small blocks, TSQR stack); with base != nullptr also carves it.
+size_t smat_layout(SMat& M, int num_sms, char* base) {
+    size_t off = layout_bytes(M.m, M.n, M.s, num_sms, &M.P, base);
+    off = (off + 1023) & ~(size_t)1023;
+    double* sb = base ? reinterpret_cast<double*>(base + off) : nullptr;
+    off += (size_t)smat_small_doubles(M.n, M.s) * sizeof(double);
+    off = (off + 1023) & ~(size_t)1023;
+    double* tw = base ? reinterpret_cast<double*>(base + off) : nullptr;
+    off += (size_t)tsqr_workspace_doubles(M.m, M.s) * sizeof(double);
+    if (base) {
+        const int n = M.n, s = M.s;
+        M.G1 = sb;
+        M.G2 = M.G1 + (i64)(n + s) * 2 * s;
+        M.Scol = M.G2 + (i64)(n + s) * 2 * s;
+        double* S0 = M.Scol + (i64)n * s;
+        M.Sd = S0 + (i64)s * s;
+        M.Yd = M.Sd + (i64)s * s;
+        M.tsqr = tw;
+    }
+    return off + 1024;
+}
+
+struct SWave {
+    std::vector<int> mats;       // indices into SplitStaged::mats
+    std::vector<SLaunch> launches;
+    SBlob blob;
+    void* blob_dev = nullptr;
+    size_t used = 0;             // bytes of the wave buffer this wave uses
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;
+};
+
+}  // namespace
+
+struct SplitStaged {
+    int count = 0, kd = 7, num_sms = kNumSMsDefault;
+    std::vector<SMat> mats;
+    std::vector<SWave> waves;
+    char* buf = nullptr;          // the wave buffer (reused by every wave)
+    size_t buf_bytes = 0;
+    int* dstatus = nullptr;       // 8 ints per matrix (not owned)
+    int* derr = nullptr;          // the batch's split-kernel error word; dtile follows it
+    int* dtile = nullptr;
+    cudaStream_t own = nullptr;
+    long long kernels = 0;
+    int nodes = 0;
+    bool device = true;           // false: a dry run (no GPU memory)
+};
+
+namespace {
+
+// Plans one wave: replays the single-matrix split driver (Engine + run_lagged_fused
+// with pyth = true) for each matrix and groups its primitives into phases.
+int plan_wave(SplitStaged& S, SWave& W) {
+    const int KD = S.kd;
+    size_t off = 0;
+    for (int i : W.mats) {
+        SMat& M = S.mats[i];
+        M.off = off;
+        char* base = S.device ? S.buf + off : nullptr;
+        M.bytes = smat_layout(M, S.num_sms, base);
+        off += (M.bytes + 4095) & ~(size_t)4095;
+        Plan& P = M.P;
+        P.kd = KD;
+        P.X = M.X; P.ld = M.ld; P.m = M.m; P.n = M.n; P.num_sms = S.num_sms;
+        P.fresh.assign((size_t)M.n, 0);
+        P.cmax_valid.assign((size_t)M.n, 0);
+        if (S.device) {
+            const int n = M.n;
+            int rc = make_map3(&P.map_col_a, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, TILE_M);
+            if (!rc) rc = make_map3(&P.map_col_b, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 32);
+            if (!rc) rc = make_map3(&P.map_col_u, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, KCH, 2);
+            for (int q = 0; q < 7 && !rc; ++q)
+                rc = make_map3(&P.map_col_a_part[q], P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 16 * (q + 1));
+            for (int q = 0; q < 3 && !rc; ++q)
+                rc = make_map3(&P.map_col_u_part[q], P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 16 * (q + 1),
+                               2);
+            if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
+            if (rc) return rc;
+        }
+    }
+    W.used = off;
+    W.launches.clear();
+    W.blob.bytes.clear();
+    // The store must read as zero where nothing is sliced (rows past m in the
+    // last 64-row chunk feed the Gram's sums) and hold no NaN bit patterns where a
+    // box reads past its columns: the wave's region is cleared first.
+    if (S.device) W.launches.push_back({kSZeroBuf, 0, 0, 0, 0, (i64)off});
+
+    auto push = [&](int kind, auto& jobs, const std::vector<int>& counts) {
+        if (jobs.empty()) return;
+        std::vector<int> prefix(jobs.size() + 1, 0);
+        for (size_t j = 0; j < jobs.size(); ++j) prefix[j + 1] = prefix[j] + counts[j];
+        SLaunch L{kind, W.blob.put(jobs), W.blob.put(prefix), (int)jobs.size(), prefix.back(), 0};
+        if (L.items > 0) W.launches.push_back(L);
+    };
+    auto push_zero = [&](std::vector<ZeroJob>& z) {
+        if (z.empty()) return;
+        SLaunch L{kSZero, W.blob.put(z), 0, (int)z.size(), (int)z.size(), 0};
+        W.launches.push_back(L);
+    };
+
+    std::vector<ZeroJob> zj;
+    std::vector<ColmaxJob> cj;
+    std::vector<int> cc;
+    std::vector<SliceJob> sj;
+    std::vector<int> sc;
+    auto flush_prepare = [&]() {
+        push_zero(zj);
+        push(kSColmax, cj, cc);
+        push(kSSlice, sj, sc);
+        zj.clear(); cj.clear(); cc.clear(); sj.clear(); sc.clear();
+    };
+    // ensure_fresh of one matrix, as jobs.
+    auto prepare = [&](SMat& M, int c_end) {
+        Plan& P = M.P;
+        int c = 0;
+        while (c < c_end) {
+            if (P.fresh[c]) { ++c; continue; }
+            int e = c;
+            while (e < c_end && !P.fresh[e] && e - c < 32 && P.cmax_valid[e] == P.cmax_valid[c]) ++e;
+            const int nc = e - c;
+            if (!P.cmax_valid[c]) {
+                zj.push_back({P.cmax + c, (int)(nc * sizeof(unsigned long long))});
+                const int nrb = (int)ceil_div(P.m, 4096);
+                cj.push_back({P.X, P.ld, P.m, c, nrb, P.cmax});
+                cc.push_back(nrb * nc);
+            }
+            const int ntile = (int)ceil_div(P.m, 128);
+            sj.push_back({P.X, P.ld, P.m, P.nrc, P.n, c, nc, ntile, P.cmax, P.cexp, P.colstore});
+            sc.push_back(ntile * (int)ceil_div(nc, 16));
+            for (int k = c; k < e; ++k) { P.fresh[k] = 1; P.cmax_valid[k] = 0; }
+            c = e;
+        }
+    };
+
+    std::vector<SplitGramJob> gj;
+    std::vector<int> gc;
+    std::vector<GramJob> rj;
+    std::vector<int> rc2;
+    // launch_gram_split's parameters for one matrix.
+    auto gram = [&](SMat& M, int na, int b0, int nb, double* C, int ldc) {
+        prepare(M, na > b0 + nb ? na : b0 + nb);
+        Plan& P = M.P;
+        GramParams gp{};
+        gp.na = na; gp.nb = nb; gp.b0 = b0; gp.m = P.m;
+        gp.numMB = (int)ceil_div(na, TILE_M);
+        gp.numNG = (int)ceil_div(nb, 32);
+        const int mbn = gp.numMB * gp.numNG;
+        gp.rc = S.num_sms / mbn > 0 ? S.num_sms / mbn : 1;
+        gp.rows_per = round_up(ceil_div(P.m, gp.rc), (i64)WIN * KCH);
+        gp.rc = (int)ceil_div(P.m, gp.rows_per);
+        gp.nrc = (int)P.nrc;
+        gp.cexp = P.cexp;
+        gp.part = P.part;
+        gp.err = nullptr;
+        gp.a_once = gp.numNG == 1 ? 1 : 0;
+        gp.alast = (int)round_up(na - (i64)(gp.numMB - 1) * TILE_M, 16);
+        SplitGramJob J;
+        std::memset(&J, 0, sizeof(J));
+        J.mapA = P.map_col_a;
+        J.mapAlast = gp.alast < TILE_M ? P.map_col_a_part[gp.alast / 16 - 1] : P.map_col_a;
+        J.mapB = P.map_col_b;
+        J.p = gp;
+        gj.push_back(J);
+        gc.push_back(mbn * gp.rc);
+        GramJob R{};
+        R.na = na; R.nb = nb; R.nchunks = gp.rc; R.part = P.part; R.C = C; R.ldc = ldc;
+        rj.push_back(R);
+        rc2.push_back((int)ceil_div((i64)na * nb, 256));
+    };
+    auto flush_gram = [&]() {
+        flush_prepare();
+        push(kSGram, gj, gc);
+        push(kSReduce, rj, rc2);
+        gj.clear(); gc.clear(); rj.clear(); rc2.clear();
+    };
+
+    std::vector<SmallJob> smj;
+    auto flush_small = [&]() {
+        if (smj.empty()) return;
+        std::vector<int> ones(smj.size(), 1);
+        push(kSSmall, smj, ones);
+        smj.clear();
+    };
+    auto pyth = [](const double* Om, int ldom, const double* A, int lda, int k, int nz, double* T, int step) {
+        SmallSub X{};
+        X.kind = kSmallPyth;
+        X.p0 = Om; X.ld0 = ldom; X.p1 = A; X.ld1 = lda; X.a = k; X.b = nz; X.out = T; X.ldo = nz; X.step = step;
+        return X;
+    };
+    auto scol = [](const double* G, int ldg, int mZ, int s, int nZ, const double* Yd, double* Scol) {
+        SmallSub X{};
+        X.kind = kSmallScol;
+        X.p0 = G; X.ld0 = ldg; X.a = mZ; X.b = s; X.c = nZ; X.p1 = Yd; X.ld1 = s; X.out = Scol; X.ldo = mZ + s;
+        return X;
+    };
+    auto rblock = [](int c0, int K, int ny, const double* A, int lda, const double* Bm, int ldb, const double* Sd,
+                     const double* Yd) {
+        SmallSub X{};
+        X.kind = kSmallRblock;
+        X.a = c0; X.b = K; X.c = ny; X.d = 0;
+        X.p0 = A; X.ld0 = lda; X.p1 = Bm; X.ld1 = ldb; X.p2 = Sd; X.ld2 = ny; X.p3 = Yd; X.ld3 = ny;
+        return X;
+    };
+
+    std::vector<ZeroJob> uz;
+    std::vector<BbuildJob> bj;
+    std::vector<int> bc;
+    std::vector<BdigitJob> dj;
+    std::vector<int> dc;
+    std::vector<SplitUpdJob> uj;
+    std::vector<int> ut;
+    // finish_update for one matrix: kin digit columns in, nout (<= 32) columns out at c0.
+    auto finish = [&](SMat& M, int kin, int c0, int nout) {
+        Plan& P = M.P;
+        dj.push_back({P.bfull, (int)P.kpad, kin - nout, nout, 32, (int)P.kpad, P.bmax, P.fexp, P.bdig});
+        dc.push_back((int)ceil_div(P.kpad, 256));
+        uz.push_back({P.cmax + c0, (int)(nout * sizeof(unsigned long long))});
+        UpdateParams up{};
+        up.nrc = (int)P.nrc;
+        up.m = P.m; up.kin = kin; up.nc = nout; up.c0 = c0; up.ld = P.ld; up.X = P.X; up.fexp = P.fexp;
+        up.cmax = P.cmax; up.err = nullptr; up.tile_ctr = nullptr;
+        up.kr_last = (int)round_up(kin - (i64)(ceil_div(kin, KCH) - 1) * KCH, 16);
+        SplitUpdJob J;
+        std::memset(&J, 0, sizeof(J));
+        J.mapA = P.map_col_u;
+        J.mapAlast = up.kr_last < KCH ? P.map_col_u_part[up.kr_last / 16 - 1] : P.map_col_u;
+        J.mapB = P.map_bdig32;
+        J.p = up;
+        uj.push_back(J);
+        ut.push_back((int)ceil_div(P.m, TILE_M));
+        for (int c = c0; c < c0 + nout; ++c) { P.fresh[c] = 0; P.cmax_valid[c] = 1; }
+    };
+    // Engine::update (launch_update_split): X[:, c0:c0+nc] = (X_c - X[:, 0:K] S) T^{-1}, c0 == K.
+    auto update = [&](SMat& M, int K, int c0, int nc, const double* Sm, int lds, const double* T, int ldt) {
+        prepare(M, K + nc);
+        Plan& P = M.P;
+        uz.push_back({P.bmax, (int)(64 * sizeof(unsigned long long))});
+        BbuildJob B{};
+        B.fused = 0; B.S = Sm; B.lds = lds; B.T = T; B.ldt = ldt; B.K = K; B.nc = nc;
+        B.cexp = P.cexp; B.Bp = P.bfull; B.ldb = (int)P.kpad; B.bmax = P.bmax;
+        bj.push_back(B);
+        bc.push_back((int)ceil_div(K + nc, 64));
+        finish(M, K + nc, c0, nc);
+    };
+    // Engine::fused_update (launch_fused_update_split).
+    auto fused = [&](SMat& M, int K, int nz, const double* G, int ldg, const double* Ty, const double* Sp,
+                     const double* Ts) {
+        const int s = M.s;
+        prepare(M, K + s + nz);
+        Plan& P = M.P;
+        uz.push_back({P.bmax, (int)(128 * sizeof(unsigned long long))});
+        BbuildJob B{};
+        B.fused = 1; B.G = G; B.ldg = ldg; B.K = K; B.s = s; B.Ty = Ty; B.Sp = Sp; B.ldsp = K + s; B.Ts = Ts;
+        B.nz = nz; B.cexp = P.cexp; B.Bp = P.bfull; B.ldb = (int)P.kpad; B.bmax = P.bmax;
+        bj.push_back(B);
+        bc.push_back((int)ceil_div(K + s + nz, 64));
+        finish(M, K + s + nz, K, s + nz);
+    };
+    auto flush_update = [&]() {
+        flush_prepare();
+        if (uj.empty()) return;
+        if (S.device) uz.push_back({S.dtile, (int)sizeof(int)});
+        push_zero(uz);
+        push(kSBbuild, bj, bc);
+        push(kSBdigit, dj, dc);
+        push(kSUpdate, uj, ut);
+        uz.clear(); bj.clear(); bc.clear(); dj.clear(); dc.clear(); uj.clear(); ut.clear();
+    };
+
+    // ---- TSQR of block 1 (the single-panel tree of launch_tsqr, per matrix) ----
+    {
+        constexpr int TR = 256;
+        struct Lv { double* ptr; i64 rows, ld; };
+        std::vector<std::vector<Lv>> lv;
+        std::vector<double*> rroot;
+        int Lmax = 0;
+        for (int i : W.mats) {
+            SMat& M = S.mats[i];
+            std::vector<Lv> v;
+            v.push_back({M.X, M.m, M.ld});
+            double* cursor = M.tsqr;
+            while (v.back().rows > TR) {
+                const i64 tiles = ceil_div(v.back().rows, TR);
+                double* next = cursor;
+                cursor = cursor ? cursor + tiles * M.s * M.s : nullptr;
+                v.push_back({next, tiles * M.s, tiles * M.s});
+            }
+            rroot.push_back(cursor);
+            Lmax = std::max(Lmax, (int)v.size() - 1);
+            lv.push_back(v);
+        }
+        const int B = (int)W.mats.size();
+        for (int l = 0; l <= Lmax; ++l) {
+            std::vector<TsqrTileJob> jobs;
+            std::vector<int> counts;
+            for (int k = 0; k < B; ++k) {
+                const SMat& M = S.mats[W.mats[k]];
+                const int L = (int)lv[k].size() - 1;
+                if (l > L) continue;
+                const Lv& v = lv[k][l];
+                TsqrTileJob J;
+                J.A = v.ptr; J.lda = v.ld; J.rows = v.rows; J.nc = M.s;
+                if (l < L) {
+                    const i64 tiles = ceil_div(v.rows, TR);
+                    J.Rst = lv[k][l + 1].ptr; J.ldr = tiles * M.s;
+                    counts.push_back((int)tiles);
+                } else {
+                    J.Rst = rroot[k]; J.ldr = M.s;
+                    counts.push_back(1);
+                }
+                jobs.push_back(J);
+            }
+            push(kSTile, jobs, counts);
+        }
+        {
+            std::vector<TsqrRootJob> jobs;
+            std::vector<int> counts;
+            for (int k = 0; k < B; ++k) {
+                const SMat& M = S.mats[W.mats[k]];
+                const Lv& v = lv[k].back();
+                TsqrRootJob J;
+                J.Q = v.ptr; J.ldq = v.ld; J.hq = (int)v.rows; J.nc = M.s;
+                J.R = rroot[k]; J.ldr = M.s; J.Rout = M.R; J.ldro = M.ldR;
+                jobs.push_back(J);
+                counts.push_back(1);
+            }
+            push(kSRoot, jobs, counts);
+        }
+        for (int l = Lmax - 1; l >= 0; --l) {
+            std::vector<TsqrApplyJob> jobs;
+            std::vector<int> counts;
+            for (int k = 0; k < B; ++k) {
+                const SMat& M = S.mats[W.mats[k]];
+                const int L = (int)lv[k].size() - 1;
+                if (l >= L) continue;
+                TsqrApplyJob J;
+                J.Q = lv[k][l].ptr; J.ldq = lv[k][l].ld; J.rows = lv[k][l].rows; J.nc = M.s; J.TR = TR;
+                J.P = lv[k][l + 1].ptr; J.ldp = lv[k][l + 1].ld;
+                jobs.push_back(J);
+                counts.push_back((int)ceil_div(J.rows, 128));
+            }
+            push(kSApply, jobs, counts);
+        }
+        for (int i : W.mats) {
+            SMat& M = S.mats[i];
+            for (int c = 0; c < M.s; ++c) { M.P.fresh[c] = 0; M.P.cmax_valid[c] = 0; }
+        }
+    }
+
+    // ---- the schedule of run_lagged_fused (pyth = true), phase by phase ----
+    const int B = (int)W.mats.size();
+    std::vector<int> nZ(B), mZ(B), ldg(B);
+    int pmax = 0;
+    for (int k = 0; k < B; ++k) pmax = std::max(pmax, S.mats[W.mats[k]].p);
+    // Phase 0: W = X_{1:2}^T X_2 (:111-114), Sdiag (:115-119), U_2 (:121-124).
+    for (int k = 0; k < B; ++k) {
+        SMat& M = S.mats[W.mats[k]];
+        gram(M, 2 * M.s, M.s, M.s, M.G2, 2 * M.s);
+    }
+    flush_gram();
+    for (int k = 0; k < B; ++k) {
+        SMat& M = S.mats[W.mats[k]];
+        SmallJob J{};
+        J.status = M.status; J.R = M.R; J.ldR = M.ldR;
+        J.sub[0] = pyth(M.G2 + M.s, 2 * M.s, M.G2, 2 * M.s, M.s, M.s, M.Sd, 1);
+        J.nsub = 1;
+        smj.push_back(J);
+    }
+    flush_small();
+    for (int k = 0; k < B; ++k) {
+        SMat& M = S.mats[W.mats[k]];
+        update(M, M.s, M.s, M.s, M.G2, 2 * M.s, M.Sd, M.s);
+    }
+    flush_update();
+    // Phase 1: the first synchronization of Q_2 (:127-147), then Q_2 and U_3.
+    for (int k = 0; k < B; ++k) {
+        SMat& M = S.mats[W.mats[k]];
+        const int s = M.s;
+        nZ[k] = M.n - s - s < s ? M.n - s - s : s;
+        const int na = 2 * s + nZ[k], nb = s + nZ[k];
+        gram(M, na, s, nb, M.G1, na);
+        ldg[k] = na;
+        mZ[k] = s;
+    }
+    flush_gram();
+    for (int k = 0; k < B; ++k) {
+        SMat& M = S.mats[W.mats[k]];
+        const int s = M.s;
+        SmallJob J{};
+        J.status = M.status; J.R = M.R; J.ldR = M.ldR;
+        J.sub[0] = pyth(M.G1 + s, ldg[k], M.G1, ldg[k], s, s, M.Yd, 1);
+        J.sub[1] = rblock(s, s, s, M.G2, 2 * s, M.G1, ldg[k], M.Sd, M.Yd);
+        J.nsub = 2;
+        if (M.p > 1) {
+            const int mScolN = mZ[k] + s;
+            J.sub[2] = scol(M.G1, ldg[k], mZ[k], s, nZ[k], M.Yd, M.Scol);
+            J.sub[3] = pyth(M.G1 + mScolN + (i64)s * ldg[k], ldg[k], M.Scol, mScolN, mScolN, nZ[k], M.Sd, 2);
+            J.nsub = 4;
+        }
+        smj.push_back(J);
+    }
+    flush_small();
+    for (int k = 0; k < B; ++k) {
+        SMat& M = S.mats[W.mats[k]];
+        const int s = M.s;
+        if (M.p <= 1) update(M, s, s, s, M.G1, ldg[k], M.Yd, s);
+        else fused(M, s, nZ[k], M.G1, ldg[k], M.Yd, M.Scol, M.Sd);
+    }
+    flush_update();
+    // Phases 2 .. pmax: block step i = phase - 1 (:152-218).
+    std::vector<int> nY(B), nZn(B);
+    for (int ph = 2; ph <= pmax; ++ph) {
+        const int i = ph - 1;
+        for (int k = 0; k < B; ++k) {
+            SMat& M = S.mats[W.mats[k]];
+            if (i > M.p - 1) continue;
+            const int s = M.s, n = M.n, mScol = mZ[k] + s;
+            int na, nb;
+            if (i < M.p - 1) {
+                nZn[k] = n - (i + 1) * s - s < s ? n - (i + 1) * s - s : s;
+                na = mScol + s + nZn[k];
+                nb = s + nZn[k];
+                nY[k] = s;
+            } else {
+                nZn[k] = nZ[k];
+                na = mScol + nZ[k];
+                nb = nZ[k];
+                nY[k] = nZ[k];
+            }
+            gram(M, na, mScol, nb, M.G1, na);
+            ldg[k] = na;
+        }
+        flush_gram();
+        for (int k = 0; k < B; ++k) {
+            SMat& M = S.mats[W.mats[k]];
+            if (i > M.p - 1) continue;
+            const int s = M.s, mScol = mZ[k] + s;
+            SmallJob J{};
+            J.status = M.status; J.R = M.R; J.ldR = M.ldR;
+            J.sub[0] = pyth(M.G1 + mScol, ldg[k], M.G1, ldg[k], mScol, nY[k], M.Yd, i + 1);
+            J.sub[1] = rblock(mScol, mScol, nY[k], M.Scol, mScol, M.G1, ldg[k], M.Sd, M.Yd);
+            J.nsub = 2;
+            if (i < M.p - 1) {
+                const int mZn = mZ[k] + s, mScolN = mZn + s;
+                J.sub[2] = scol(M.G1, ldg[k], mZn, s, nZn[k], M.Yd, M.Scol);
+                J.sub[3] = pyth(M.G1 + mScolN + (i64)s * ldg[k], ldg[k], M.Scol, mScolN, mScolN, nZn[k], M.Sd, i + 2);
+                J.nsub = 4;
+            }
+            smj.push_back(J);
+        }
+        flush_small();
+        for (int k = 0; k < B; ++k) {
+            SMat& M = S.mats[W.mats[k]];
+            if (i > M.p - 1) continue;
+            const int s = M.s, mScol = mZ[k] + s;
+            if (i < M.p - 1) fused(M, mScol, nZn[k], M.G1, ldg[k], M.Yd, M.Scol, M.Sd);
+            else update(M, mScol, mScol, nY[k], M.G1, ldg[k], M.Yd, nY[k]);
+            mZ[k] += s;
+            nZ[k] = nZn[k];
+        }
+        flush_update();
+    }
+    return 0;
+}
+
+int enqueue_wave(SplitStaged& S, SWave& W, cudaStream_t st) {
+    char* jb = static_cast<char*>(W.blob_dev);
+    const long long k0 = g_launch_count;
+    const int KD = S.kd;
+    GramParams g0{};
+    g0.err = S.derr;
+    UpdateParams u0{};
+    u0.err = S.derr;
+    u0.tile_ctr = S.dtile;
+    CUtensorMap none;
+    std::memset(&none, 0, sizeof(none));
+    for (const SLaunch& L : W.launches) {
+        const int* pre = reinterpret_cast<const int*>(jb + L.prefix_off);
+        const unsigned items = (unsigned)L.items;
+        int rc = 0;
+        switch (L.kind) {
+            case kSZeroBuf: rc = zero_async(S.buf, (size_t)L.bytes, st); break;
+            case kSZero:
+                zero_list<<<items, 256, 0, st>>>(reinterpret_cast<const ZeroJob*>(jb + L.job_off));
+                ++g_launch_count;
+                break;
+            case kSColmax:
+                colmax_batched<<<items, 256, 0, st>>>(reinterpret_cast<const ColmaxJob*>(jb + L.job_off), pre, L.njobs);
+                ++g_launch_count;
+                break;
+            case kSSlice:
+                if (KD == 6)
+                    slice_batched<6><<<items, 128, 0, st>>>(reinterpret_cast<const SliceJob*>(jb + L.job_off), pre,
+                                                            L.njobs);
+                else
+                    slice_batched<7><<<items, 128, 0, st>>>(reinterpret_cast<const SliceJob*>(jb + L.job_off), pre,
+                                                            L.njobs);
+                ++g_launch_count;
+                break;
+            case kSGram: {
+                const auto* J = reinterpret_cast<const SplitGramJob*>(jb + L.job_off);
+                if (KD == 6)
+                    gram_tc_kernel<6, true><<<items, NTHREADS, SmemLayout<32, 6>::BYTES, st>>>(none, none, none, g0, J,
+                                                                                             pre, L.njobs);
+                else
+                    gram_tc_kernel<7, true><<<items, NTHREADS, SmemLayout<32, 7>::BYTES, st>>>(none, none, none, g0, J,
+                                                                                             pre, L.njobs);
+                ++g_launch_count;
+                break;
+            }
+            case kSReduce:
+                rc = launch_gram_reduce_batched(reinterpret_cast<const GramJob*>(jb + L.job_off), pre, L.njobs,
+                                                L.items, st);
+                break;
+            case kSSmall:
+                rc = launch_small_batched(reinterpret_cast<const SmallJob*>(jb + L.job_off), L.njobs, st);
+                break;
+            case kSBbuild:
+                bbuild_batched<<<items, 256, kBbuildSmem, st>>>(reinterpret_cast<const BbuildJob*>(jb + L.job_off), pre,
+                                                               L.njobs);
+                ++g_launch_count;
+                break;
+            case kSBdigit:
+                if (KD == 6)
+                    bdigit_batched<6><<<items, 256, 0, st>>>(reinterpret_cast<const BdigitJob*>(jb + L.job_off), pre,
+                                                             L.njobs);
+                else
+                    bdigit_batched<7><<<items, 256, 0, st>>>(reinterpret_cast<const BdigitJob*>(jb + L.job_off), pre,
+                                                             L.njobs);
+                ++g_launch_count;
+                break;
+            case kSUpdate: {
+                const auto* J = reinterpret_cast<const SplitUpdJob*>(jb + L.job_off);
+                const unsigned grid = items < (unsigned)S.num_sms ? items : (unsigned)S.num_sms;
+                if (KD == 6)
+                    update_tc_kernel<32, 6, true><<<grid, NTHREADS, SmemLayout<32, 6>::BYTES, st>>>(none, none, none, u0,
+                                                                                                   J, pre, L.njobs);
+                else
+                    update_tc_kernel<32, 7, true><<<grid, NTHREADS, SmemLayout<32, 7>::BYTES, st>>>(none, none, none, u0,
+                                                                                                   J, pre, L.njobs);
+                ++g_launch_count;
+                break;
+            }
+            case kSTile:
+                rc = launch_tsqr_tile_batched(reinterpret_cast<const TsqrTileJob*>(jb + L.job_off), pre, L.njobs,
+                                              L.items, 16, st);
+                break;
+            case kSRoot:
+                rc = launch_tsqr_root_batched(reinterpret_cast<const TsqrRootJob*>(jb + L.job_off), L.njobs, st);
+                break;
+            case kSApply:
+                rc = launch_tsqr_apply_batched(reinterpret_cast<const TsqrApplyJob*>(jb + L.job_off), pre, L.njobs,
+                                               L.items, 16, st);
+                break;
+            default: rc = (int)cudaErrorInvalidValue;
+        }
+        if (!rc) rc = (int)cudaGetLastError();
+        if (rc) return rc;
+    }
+    W.kernels = g_launch_count - k0;
+    return 0;
+}
+
+void free_staged(SplitStaged* S) {
+    if (!S) return;
+    for (SWave& W : S->waves) {
+        if (W.exec) cudaGraphExecDestroy(W.exec);
+        if (W.graph) cudaGraphDestroy(W.graph);
+        if (W.blob_dev) cudaFree(W.blob_dev);
+    }
+    if (S->buf) cudaFree(S->buf);
+    if (S->derr) cudaFree(S->derr);
+    if (S->own) cudaStreamDestroy(S->own);
+    delete S;
+}
+
+// Matrices into waves, in batch order: a wave takes matrices while their regions
+// fit in `budget` bytes (at least one matrix per wave).
+void assign_waves(SplitStaged& S, long long budget) {
+    S.waves.clear();
+    SWave cur;
+    size_t used = 0;
+    for (int i = 0; i < S.count; ++i) {
+        SMat& M = S.mats[i];
+        const size_t b = (smat_layout(M, S.num_sms, nullptr) + 4095) & ~(size_t)4095;
+        if (!cur.mats.empty() && budget > 0 && (long long)(used + b) > budget) {
+            S.waves.push_back(std::move(cur));
+            cur = SWave();
+            used = 0;
+        }
+        cur.mats.push_back(i);
+        used += b;
+    }
+    if (!cur.mats.empty()) S.waves.push_back(std::move(cur));
+}
+
+int fill_smats(SplitStaged& S, int count, const int* m, const int* n, const int* s, double* const* dX,
+               const long long* ldX, double* const* dR, const int* ldR, int* dstatus) {
+    S.count = count;
+    S.mats.resize(count);
+    for (int b = 0; b < count; ++b) {
+        SMat& M = S.mats[b];
+        M.b = b; M.m = m[b]; M.n = n[b]; M.s = s[b];
+        M.ld = ldX ? ldX[b] : m[b];
+        M.X = dX ? dX[b] : nullptr;
+        M.R = dR ? dR[b] : nullptr;
+        M.ldR = ldR ? ldR[b] : n[b];
+        M.status = dstatus ? dstatus + 8 * (i64)b : nullptr;
+        if (M.s < 1 || M.s > 16 || M.n < 2 * M.s || M.m < M.n || M.ld < M.m || M.ldR < M.n || M.m < TILE_M) return 2;
+        M.p = (M.n - M.s + M.s - 1) / M.s;
+    }
+    return 0;
+}
+
+}  // namespace
+
+bool split_staged_supported(int variant, int count, const int* s) {
+    if (variant != ORTH_GB300_BCGSI2P1S) return false;
+    for (int b = 0; b < count; ++b)
+        if (s[b] < 1 || s[b] > 16) return false;
+    return true;
+}
+
+int split_staged_create(int count, const int* m, const int* n, const int* s, double* const* dX,
+                        const long long* ldX, double* const* dR, const int* ldR, int kd, int* dstatus,
+                        long long budget, cudaStream_t st, SplitStaged** out) {
+    *out = nullptr;
+    SplitStaged* S = new SplitStaged();
+    S->kd = kd;
+    S->dstatus = dstatus;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&S->num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        free_staged(S);
+        return 3;
+    }
+    int rc = fill_smats(*S, count, m, n, s, dX, ldX, dR, ldR, dstatus);
+    if (rc) { free_staged(S); return rc; }
+    // Shared-memory limits of the batched kernels on this device.
+    rc = set_smem(gram_tc_kernel<6, true>, SmemLayout<32, 6>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<7, true>, SmemLayout<32, 7>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<32, 6, true>, SmemLayout<32, 6>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<32, 7, true>, SmemLayout<32, 7>::BYTES);
+    if (!rc) rc = set_smem(bbuild_batched, (int)kBbuildSmem);
+    if (!rc) rc = tsqr_tile_batched_prepare();
+    if (rc) { free_staged(S); return 3; }
+    if (budget < 0) {
+        size_t fb = 0, tb = 0;
+        if (cudaMemGetInfo(&fb, &tb) != cudaSuccess) { free_staged(S); return 3; }
+        budget = (long long)((double)fb * 0.85) - (256LL << 20);
+        if (budget < (256LL << 20)) budget = 256LL << 20;
+    }
+    assign_waves(*S, budget);
+    size_t need = 0;
+    for (SWave& W : S->waves) {
+        size_t u = 0;
+        for (int i : W.mats) u += (smat_layout(S->mats[i], S->num_sms, nullptr) + 4095) & ~(size_t)4095;
+        need = std::max(need, u);
+    }
+    S->buf_bytes = need;
+    if (cudaMalloc(&S->buf, need) != cudaSuccess || cudaMalloc(&S->derr, 64) != cudaSuccess ||
+        cudaMemset(S->derr, 0, 64) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&S->own, cudaStreamNonBlocking) != cudaSuccess) {
+        (void)cudaGetLastError();
+        free_staged(S);
+        return 3;
+    }
+    S->dtile = S->derr + 1;
+    for (SWave& W : S->waves) {
+        rc = plan_wave(*S, W);
+        if (rc) { free_staged(S); return 3; }
+        if (cudaMalloc(&W.blob_dev, W.blob.bytes.size() + 128) != cudaSuccess ||
+            cudaMemcpy(W.blob_dev, W.blob.bytes.data(), W.blob.bytes.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            free_staged(S);
+            return 3;
+        }
+    }
+    // Capture each wave; the first also clears the status words and the error
+    // word, the last copies the error word into every matrix's status.
+    if (cudaStreamSynchronize(st) != cudaSuccess) { free_staged(S); return 3; }
+    for (size_t w = 0; w < S->waves.size(); ++w) {
+        SWave& W = S->waves[w];
+        if (cudaStreamBeginCapture(S->own, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { free_staged(S); return 3; }
+        rc = 0;
+        if (w == 0) {
+            rc = zero_async(S->dstatus, (size_t)S->count * 8 * sizeof(int), S->own);
+            if (!rc) rc = zero_async(S->derr, sizeof(int), S->own);
+        }
+        if (!rc) rc = enqueue_wave(*S, W, S->own);
+        if (!rc && w + 1 == S->waves.size()) {
+            spread_error<<<(unsigned)ceil_div(S->count, 256), 256, 0, S->own>>>(S->derr, S->dstatus, S->count);
+            ++g_launch_count;
+            rc = (int)cudaGetLastError();
+        }
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(S->own, &g);
+        if (rc || ce != cudaSuccess || !g) {
+            if (g) cudaGraphDestroy(g);
+            free_staged(S);
+            return 3;
+        }
+        W.graph = g;
+        if (cudaGraphInstantiate(&W.exec, g, 0) != cudaSuccess) { free_staged(S); return 3; }
+        size_t nodes = 0;
+        cudaGraphGetNodes(g, nullptr, &nodes);
+        S->nodes += (int)nodes;
+        S->kernels += W.kernels + (w == 0 ? 2 : 0) + (w + 1 == S->waves.size() ? 1 : 0);
+    }
+    *out = S;
+    return 0;
+}
+
+int split_staged_run(SplitStaged* S, cudaStream_t st) {
+    if (!S) return 2;
+    for (SWave& W : S->waves)
+        if (cudaGraphLaunch(W.exec, st) != cudaSuccess) return 3;
+    g_launch_count += S->kernels;
+    return 0;
+}
+
+void split_staged_destroy(SplitStaged* S) { free_staged(S); }
+
+void split_staged_info(const SplitStaged* S, long long* kernels, long long* bytes, int* nodes, int* waves) {
+    if (!S) return;
+    if (kernels) *kernels = S->kernels;
+    if (bytes) *bytes = (long long)S->buf_bytes;
+    if (nodes) *nodes = S->nodes;
+    if (waves) *waves = (int)S->waves.size();
+}
+
+int split_staged_dry_run(int count, const int* m, const int* n, const int* s, long long budget, int* waves,
+                         long long* kernels, long long* bytes) {
+    SplitStaged S;
+    S.device = false;
+    S.num_sms = kNumSMsDefault;
+    int rc = fill_smats(S, count, m, n, s, nullptr, nullptr, nullptr, nullptr, nullptr);
+    if (rc) return rc;
+    assign_waves(S, budget);
+    long long k = 4;   // the status and error clears, the error spread, one buffer clear per wave below
+    size_t need = 0;
+    for (SWave& W : S.waves) {
+        plan_wave(S, W);
+        k += (long long)W.launches.size() + 1;
+        need = std::max(need, W.used);
+    }
+    k -= 1;
+    if (waves) *waves = (int)S.waves.size();
+    if (kernels) *kernels = k;
+    if (bytes) *bytes = (long long)need;
+    return 0;
+}
+
 }  // namespace bcgs
