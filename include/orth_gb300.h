@@ -191,7 +191,8 @@ void orth_gb300_set_gram_chunk_rows(long long rows);
  *   - ORTH_GB300_BCGSI2P1S with every s[b] <= 16 (the default form): staged
  *     graphs. The matrices are taken in order into waves whose digit stores
  *     (14 bytes per element) and scratch fit in 85 % of the free device memory at
- *     creation; in a wave every stage of the split driver (slicing, the
+ *     creation (or in ORTH_GB300_SPLIT_WAVE_BYTES bytes, when that environment
+ *     variable is set); in a wave every stage of the split driver (slicing, the
  *     tensor-core Gram and its reduction, the small FP64 operations, the factor,
  *     its digits, the fused update; the TSQR of block 1) is one launch over all
  *     its matrices, and each wave is one captured CUDA graph; a run replays the

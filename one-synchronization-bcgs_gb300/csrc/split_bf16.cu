@@ -38,6 +38,7 @@
 // error word and the kernel winds down.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -1652,6 +1653,7 @@ int plan_wave(SplitStaged& S, SWave& W) {
     std::vector<int> gc;
     std::vector<GramJob> rj;
     std::vector<int> rc2;
+    bool too_big = false;   // a Gram's partials would not fit the matrix's buffer
     // launch_gram_split's parameters for one matrix.
     auto gram = [&](SMat& M, int na, int b0, int nb, double* C, int ldc) {
         prepare(M, na > b0 + nb ? na : b0 + nb);
@@ -1670,6 +1672,7 @@ int plan_wave(SplitStaged& S, SWave& W) {
         gp.err = nullptr;
         gp.a_once = gp.numNG == 1 ? 1 : 0;
         gp.alast = (int)round_up(na - (i64)(gp.numMB - 1) * TILE_M, 16);
+        if ((i64)gp.rc * na * nb > P.part_doubles) too_big = true;
         SplitGramJob J;
         std::memset(&J, 0, sizeof(J));
         J.mapA = P.map_col_a;
@@ -1976,7 +1979,7 @@ int plan_wave(SplitStaged& S, SWave& W) {
         }
         flush_update();
     }
-    return 0;
+    return too_big ? (int)cudaErrorInvalidValue : 0;
 }
 
 int enqueue_wave(SplitStaged& S, SWave& W, cudaStream_t st) {
@@ -2161,6 +2164,10 @@ int split_staged_create(int count, const int* m, const int* n, const int* s, dou
     if (!rc) rc = tsqr_tile_batched_prepare();
     if (rc) { free_staged(S); return 3; }
     if (budget < 0) {
+        const char* e = getenv("ORTH_GB300_SPLIT_WAVE_BYTES");
+        if (e && atoll(e) > 0) budget = atoll(e);
+    }
+    if (budget < 0) {
         size_t fb = 0, tb = 0;
         if (cudaMemGetInfo(&fb, &tb) != cudaSuccess) { free_staged(S); return 3; }
         budget = (long long)((double)fb * 0.85) - (256LL << 20);
@@ -2255,7 +2262,7 @@ int split_staged_dry_run(int count, const int* m, const int* n, const int* s, lo
     long long k = 4;   // the status and error clears, the error spread, one buffer clear per wave below
     size_t need = 0;
     for (SWave& W : S.waves) {
-        plan_wave(S, W);
+        if (plan_wave(S, W)) return 2;
         k += (long long)W.launches.size() + 1;
         need = std::max(need, W.used);
     }

@@ -133,26 +133,37 @@ def test_batch_rejects_bad_arguments(lib):
     assert orth.Batch([3000], [32], [8], [x.data_ptr()], [r.data_ptr()], variant="bcgsi2").rc == 4
 
 
-@pytest.mark.parametrize("variant", ["bcgsi2P1s", "bcgsi21s"])
-def test_split_batch_matches_single_split_runs(lib, variant):
-    """Split-precision batches run each matrix through the single-matrix tensor-core
-    driver: bit-identical to orth_gb300_run_dev per matrix, and within 10x of the
-    FP64 path's LOO and residual; breakdowns are reported per matrix."""
+@pytest.mark.parametrize("variant,form", [("bcgsi2P1s", "staged"), ("bcgsi2P1s", "streams"),
+                                          ("bcgsi21s", "streams")])
+def test_split_batch_matches_single_split_runs(lib, variant, form):
+    """Split-precision batches: BCGSI+P-1S with s <= 16 runs as staged graphs (one
+    launch per stage for all matrices), other variants (or on request) through the
+    single-matrix tensor-core driver per matrix. Either way each matrix's Q and R are
+    bit-identical to orth_gb300_run_dev's, within 10x of the FP64 path's LOO and
+    residual; breakdowns are reported per matrix; two runs give the same bits."""
     torch = pytest.importorskip("torch")
     ms, ns, ss, mats = _batch(seed=21, count=10, m_hi=20000, p_hi=6, kappa_hi=1e6)
     dX = _to_dev(torch, mats)
     dR = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for n in ns]
     st = torch.cuda.current_stream().cuda_stream
     plan = orth.Batch(ms, ns, ss, [x.data_ptr() for x in dX], [r.data_ptr() for r in dR],
-                      precision=orth.SPLIT_BF16, stream=st, variant=variant)
+                      precision=orth.SPLIT_BF16, stream=st, variant=variant, streams=(form == "streams"))
     assert plan.rc == 0
-    for rep in range(2):                       # two runs: stores re-zeroed per shape
+    if form == "staged":
+        # launches per run: a few hundred per wave, not about a hundred per matrix per step
+        assert 0 < plan.info()["launches"] < 400, plan.info()
+    for rep in range(2):
         for b, X in enumerate(mats):
             dX[b].copy_(torch.from_numpy(np.ascontiguousarray(X.T)))
             dR[b].zero_()
         assert plan.run(st) == 0
         rc, steps, _, _ = plan.status()
         assert rc == 0
+    _check_split_batch(torch, variant, ms, ns, ss, mats, dX, dR, steps, st)
+    plan.close()
+
+
+def _check_split_batch(torch, variant, ms, ns, ss, mats, dX, dR, steps, st):
     for b, X in enumerate(mats):
         m, n, s = ms[b], ns[b], ss[b]
         outs = {}
@@ -163,10 +174,35 @@ def test_split_batch_matches_single_split_runs(lib, variant):
             assert rc1 == 0
             outs[prec] = (x1.cpu().numpy().T, r1.cpu().numpy().T, st1["breakdown_step"])
         Qs, Rs, step_s = outs[orth.SPLIT_BF16]
-        assert np.array_equal(dX[b].cpu().numpy().T, Qs) and np.array_equal(dR[b].cpu().numpy().T, Rs), b
+        assert np.array_equal(dX[b].cpu().numpy().T, Qs), b
+        assert np.array_equal(np.triu(dR[b].cpu().numpy().T), np.triu(Rs)), b
         assert steps[b] == step_s
         Qf, Rf, _ = outs[orth.FP64]
         if step_s == 0:
             assert port.loo_2(Qs) <= 10 * max(port.loo_2(Qf), 1e-15)
             assert port.rel_residual(X, Qs, np.triu(Rs)) <= 10 * max(port.rel_residual(X, Qf, np.triu(Rf)), 1e-15)
+
+
+def test_split_staged_batch_several_waves(lib, monkeypatch):
+    """A wave budget smaller than the batch (ORTH_GB300_SPLIT_WAVE_BYTES) splits the
+    staged plan into several waves, replayed in order; every matrix is still
+    bit-identical to its single run, including a p = 1 matrix (n = 2s) and
+    breakdowns at high kappa."""
+    torch = pytest.importorskip("torch")
+    ms, ns, ss, mats = _batch(seed=5, count=9, m_hi=12000, p_hi=5, kappa_hi=1e10)
+    ms.append(4000); ns.append(32); ss.append(16)
+    mats.append(inputs.graded_host(4000, 32, 1e3, seed=99))
+    est = orth.split_batch_dry_run(ms, ns, ss, 1 << 60)
+    monkeypatch.setenv("ORTH_GB300_SPLIT_WAVE_BYTES", str(max(1, est["bytes"] // 3)))
+    assert orth.split_batch_dry_run(ms, ns, ss, max(1, est["bytes"] // 3))["waves"] >= 3
+    dX = _to_dev(torch, mats)
+    dR = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for n in ns]
+    st = torch.cuda.current_stream().cuda_stream
+    plan = orth.Batch(ms, ns, ss, [x.data_ptr() for x in dX], [r.data_ptr() for r in dR],
+                      precision=orth.SPLIT_BF16, stream=st)
+    assert plan.rc == 0
+    assert plan.run(st) == 0
+    rc, steps, _, nbroken = plan.status()
+    assert rc == 0
+    _check_split_batch(torch, "bcgsi2P1s", ms, ns, ss, mats, dX, dR, steps, st)
     plan.close()

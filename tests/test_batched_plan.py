@@ -102,3 +102,22 @@ def test_split_batch_plan_fits_free_memory_and_caps(lib):
     three = orth.split_batch_plan(ms[:3], ns[:3], ss[:3])
     assert three["slots"] == 3 and sorted(three["slot_of"]) == [0, 1, 2]
     assert orth.split_batch_plan([], [], [])["slots"] == 0
+
+
+def test_split_staged_dry_run_config4():
+    """The staged split-precision plan of the config-4 batch (4096 matrices): a few
+    hundred launches per wave (not about a hundred per matrix), more waves for a
+    smaller budget, and s > 16 refused (the staged form's limit)."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    ms, ns, ss, _ = bench.batch_shapes(4096, 2024)
+    big = orth.split_batch_dry_run(ms, ns, ss, 80 << 30)
+    small = orth.split_batch_dry_run(ms, ns, ss, 20 << 30)
+    assert big["rc"] == 0 and small["rc"] == 0
+    assert small["waves"] > big["waves"] >= 2
+    for d in (big, small):
+        assert d["launches"] / d["waves"] < 250, d
+        assert d["bytes"] <= (80 << 30)
+    assert orth.split_batch_dry_run([3000], [64], [32], 1 << 30)["rc"] == 4
