@@ -634,7 +634,7 @@ def run_batched(args, rank, world, local_rank):
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": None,
                 "note": "whole batch: algorithmic FP64 bytes 8m[sP(P-1)/2 + 4n] per matrix / run time; "
-                        "matrices run through the single-matrix tensor-core driver on up to 16 concurrent streams",
+                        "staged tensor-core plan (one launch per stage over each wave's matrices)",
                 "tflops_fp64_equivalent": round(flops / (ms_run * 1e-3) / 1e12, 3)}
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -660,8 +660,8 @@ def run_batched(args, rank, world, local_rank):
         "config": {"workload": (f"batched bcgsi2P1s, {count} matrices (seed {args.batch_seed}), FP64, "
                                 f"one CUDA graph of {info['launches']} launches per step") if bprec == orth.FP64 else
                                (f"batched bcgsi2P1s, {count} matrices (seed {args.batch_seed}), split_bf16x7, "
-                                f"per-matrix tensor-core QRs on up to 16 concurrent streams ({info['launches']} launches "
-                                f"per step)"),
+                                f"staged: waves of matrices, one launch per stage over a wave, one captured CUDA "
+                                f"graph per wave ({info['launches']} launches per step)"),
                    "batch": count, "batch_requested": args.batch, "elements": int(offs[-1]),
                    "tuned_panel_rows": {str(k): v for k, v in info["tuned"].items()},
                    "l2": f"inputs ({8 * int(offs[-1]) / 1e9:.0f} GB) larger than L2; no flush",
