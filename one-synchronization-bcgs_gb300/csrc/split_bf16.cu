@@ -29,7 +29,8 @@
 // factor, so the triangular scaling also runs on the tensor cores.
 //
 // Kernels are warp-specialized (warp 0: TMA producer, warp 1: MMA issuer + TMEM
-// owner, warps 2-9: epilogue, two threads per TMEM lane), with an A-tile ring of
+// owner, then the epilogue: in the Gram warps 2-9, two threads per TMEM lane; in
+// the update warps 2-17, four threads per TMEM lane), with an A-tile ring of
 // 16 KB slots, a B ring, and two TMEM accumulators so the epilogue of one window
 // overlaps the MMAs of the next. The update is persistent and takes row tiles from
 // a per-launch counter; the Gram's M-block CTAs of one row range run side by side
@@ -64,8 +65,13 @@ constexpr int WIN = 4;         // chunks per accumulation window (256 summation 
 constexpr int RA = 8;          // A ring depth (16 KB slots)
 constexpr int RB = 2;          // B ring depth
 constexpr int A_SLOT = TILE_M * KCH * 2;   // 16 KB
-constexpr int NTHREADS = 320;  // 10 warps: producer, MMA, 8 epilogue
-constexpr int NEPI = 256;      // epilogue threads (two per TMEM lane)
+constexpr int NTHREADS = 320;  // Gram: 10 warps: producer, MMA, 8 epilogue
+constexpr int NEPI = 256;      // Gram: epilogue threads (two per TMEM lane)
+// The update's epilogue drains and assembles every output of every row tile (the
+// Gram's only once per CTA), so it has four threads per TMEM lane: 18 warps.
+constexpr int UEPW = 4;                     // update: epilogue threads per TMEM lane
+constexpr int UNEPI = 128 * UEPW;           // update: epilogue threads
+constexpr int UTHREADS = 64 + UNEPI;        // update: producer + MMA warps + epilogue
 
 // ---------------------------------------------------------------------------
 // Digit extraction: x -> KD balanced base-256 digits of x * 2^{-e} (|x| < 2^e).
@@ -447,15 +453,16 @@ static_assert(sizeof(Bars) <= 512, "barrier block exceeds its shared-memory rese
 // integer mid (weight 2^-24 relative to hi's unit), and groups >= 6 (weight <=
 // 2^-48) into FP32. Each TMEM value is an integer below 2^24.6 (at most 3 products
 // of |digit| <= 2^7 per summation step, 256 steps per window).
-template <int NB, int KD>
+template <int NB, int KD, int NH = NB / 2>
 __device__ __forceinline__ void accumulate_window(uint32_t taddr, int col0, long long* hi, long long* mid,
                                                   float* lo) {
-    constexpr int NH = NB / 2;   // columns of this thread's half
+    // NH: columns of this thread's part of the row (16, 8 or 4)
 #pragma unroll
     for (int g = 0; g < KD; ++g) {
         float v[NH];
-        if (NH == 16) tc::tmem_ld16(taddr + (uint32_t)(g * NB + col0), v);
-        else tc::tmem_ld8(taddr + (uint32_t)(g * NB + col0), v);
+        if constexpr (NH == 16) tc::tmem_ld16(taddr + (uint32_t)(g * NB + col0), v);
+        else if constexpr (NH == 8) tc::tmem_ld8(taddr + (uint32_t)(g * NB + col0), v);
+        else tc::tmem_ld4(taddr + (uint32_t)(g * NB + col0), v);
         if (g < 3) {
             const int sh = 8 * (2 - g);
 #pragma unroll
@@ -569,7 +576,8 @@ __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uin
 }
 
 template <int NB, int KD>
-__device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint8_t*& sB, uint32_t* tmem_slot) {
+__device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint8_t*& sB, uint32_t* tmem_slot,
+                                           int nepi = NEPI) {
     using L = SmemLayout<NB, KD>;
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     sA = base + L::A_OFF;
@@ -579,10 +587,10 @@ __device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint
     if (threadIdx.x == 0) {
         for (int i = 0; i < RA; ++i) { tc::mbar_init(&bars->a_full[i], 1); tc::mbar_init(&bars->a_empty[i], 1); }
         for (int i = 0; i < RB; ++i) { tc::mbar_init(&bars->b_full[i], 1); tc::mbar_init(&bars->b_empty[i], 1); }
-        for (int i = 0; i < 2; ++i) { tc::mbar_init(&bars->t_full[i], 1); tc::mbar_init(&bars->t_empty[i], NEPI); }
+        for (int i = 0; i < 2; ++i) { tc::mbar_init(&bars->t_full[i], 1); tc::mbar_init(&bars->t_empty[i], (uint32_t)nepi); }
         tc::mbar_init(&bars->drain, 1);
         // Tile-number ring: one producer; the MMA thread and the 8 epilogue warps read.
-        for (int i = 0; i < RQ; ++i) { tc::mbar_init(&bars->q_full[i], 1); tc::mbar_init(&bars->q_empty[i], 1 + NEPI / 32); }
+        for (int i = 0; i < RQ; ++i) { tc::mbar_init(&bars->q_full[i], 1); tc::mbar_init(&bars->q_empty[i], (uint32_t)(1 + nepi / 32)); }
         tc::fence_mbar_init();
     }
     if (warp == 1) tc::tmem_alloc(tmem_slot, (uint32_t)L::TMEM_ALLOC);
@@ -780,7 +788,7 @@ struct SplitUpdJob {    // the CUtensorMap members keep the struct 64-byte align
 // order, so its jobs come in increasing order too; the epilogue writes a job's
 // column maxima when the next job starts.
 template <int NB, int KD, bool BATCH>
-__global__ void __launch_bounds__(NTHREADS, 1)
+__global__ void __launch_bounds__(UTHREADS, 1)
 update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapAlast,
                  const __grid_constant__ CUtensorMap mapB, UpdateParams p0, const SplitUpdJob* __restrict__ jobs,
                  const int* __restrict__ tprefix, int njobs) {
@@ -790,7 +798,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     __shared__ volatile int abort_flag;
     uint8_t *sA, *sB;
     if (threadIdx.x == 0) abort_flag = 0;
-    Bars* bars = setup_cta<NB, KD>(smem_raw, sA, sB, &tmem_slot);
+    Bars* bars = setup_cta<NB, KD>(smem_raw, sA, sB, &tmem_slot, UNEPI);
     const uint32_t tmem = tmem_slot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -901,9 +909,9 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
             tc::mma_commit(&bars->drain);
         }
     } else {
-        constexpr int NH = NB / 2;
-        const int quarter = warp & 3;
-        const int half = (warp - 2) >> 2;
+        constexpr int NH = NB / UEPW;   // output columns per thread
+        const int quarter = warp & 3;   // TMEM lane quarter this warp may access
+        const int half = (warp - 2) >> 2;   // which NH-column part of the row
         const int rloc = quarter * 32 + lane;
         int wc = 0;
         bool ok = true;
@@ -962,7 +970,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
                 if (!tc::mbar_wait(&bars->t_full[buf], tph, &abort_flag, p0.err, 42)) { ok = false; break; }
                 tc::tc_fence_after();
                 const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * L::TMEM_COLS_PER_BUF);
-                accumulate_window<NB, KD>(taddr, half * NH, hi, mid, lo);
+                accumulate_window<NB, KD, NH>(taddr, half * NH, hi, mid, lo);
                 tc::tc_fence_before();
                 tc::mbar_arrive(&bars->t_empty[buf]);
             }
@@ -1319,7 +1327,7 @@ static int finish_update(double* X, i64 ld, i64 m, int kin, int c0, int nc, int 
         const int ntiles = (int)ceil_div(m, TILE_M);
         const int grid = ntiles < num_sms ? ntiles : num_sms;
 #define BCGS_UPD(NBT, KDT) \
-        update_tc_kernel<NBT, KDT, false><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(                 \
+        update_tc_kernel<NBT, KDT, false><<<grid, UTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(                 \
             P.map_col_u, ulast_map, P.map_bdig##NBT, up, nullptr, nullptr, 0)
         if (NB == 16) {
             if (P.kd == 6) BCGS_UPD(16, 6); else BCGS_UPD(16, 7);
@@ -2052,10 +2060,10 @@ int enqueue_wave(SplitStaged& S, SWave& W, cudaStream_t st) {
                 const auto* J = reinterpret_cast<const SplitUpdJob*>(jb + L.job_off);
                 const unsigned grid = items < (unsigned)S.num_sms ? items : (unsigned)S.num_sms;
                 if (KD == 6)
-                    update_tc_kernel<32, 6, true><<<grid, NTHREADS, SmemLayout<32, 6>::BYTES, st>>>(none, none, none, u0,
+                    update_tc_kernel<32, 6, true><<<grid, UTHREADS, SmemLayout<32, 6>::BYTES, st>>>(none, none, none, u0,
                                                                                                    J, pre, L.njobs);
                 else
-                    update_tc_kernel<32, 7, true><<<grid, NTHREADS, SmemLayout<32, 7>::BYTES, st>>>(none, none, none, u0,
+                    update_tc_kernel<32, 7, true><<<grid, UTHREADS, SmemLayout<32, 7>::BYTES, st>>>(none, none, none, u0,
                                                                                                    J, pre, L.njobs);
                 ++g_launch_count;
                 break;
