@@ -448,33 +448,72 @@ struct Bars {
 };
 static_assert(sizeof(Bars) <= 512, "barrier block exceeds its shared-memory reservation");
 
+// acc + a * b, 32 x 32 -> 64-bit signed, in one multiply-add.
+__device__ __forceinline__ long long mad_wide(int a, int b, long long acc) {
+    long long d;
+    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(acc));
+    return d;
+}
+
+// Adds TMEM group g's values v[0..NH) into the accumulators (see accumulate_window).
+template <int NH>
+__device__ __forceinline__ void add_group(int g, const float* v, long long* hi, long long* mid, float* lo) {
+    if (g < 3) {
+        const int f = 1 << (8 * (2 - g));
+#pragma unroll
+        for (int q = 0; q < NH; ++q) hi[q] = mad_wide(__float2int_rn(v[q]), f, hi[q]);
+    } else if (g < 6) {
+        const int f = 1 << (8 * (5 - g));
+#pragma unroll
+        for (int q = 0; q < NH; ++q) mid[q] = mad_wide(__float2int_rn(v[q]), f, mid[q]);
+    } else {
+        const float w = __int_as_float((127 - 8 * (g - 6)) << 23);  // 2^{-8(g-6)}
+#pragma unroll
+        for (int q = 0; q < NH; ++q) lo[q] = fmaf(v[q], w, lo[q]);
+    }
+}
+
 // Per-window epilogue accumulation of the TMEM groups: groups 0-2 (weights 1,
 // 2^-8, 2^-16) into the exact 64-bit integer hi, groups 3-5 into the exact 64-bit
 // integer mid (weight 2^-24 relative to hi's unit), and groups >= 6 (weight <=
 // 2^-48) into FP32. Each TMEM value is an integer below 2^24.6 (at most 3 products
-// of |digit| <= 2^7 per summation step, 256 steps per window).
+// of |digit| <= 2^7 per summation step, 256 steps per window). With 8 or 4
+// columns per thread the group loads go out in batches (4 groups, or all) under
+// one wait each; with 16 (the Gram, not bound by its epilogue) each load waits
+// on its own.
 template <int NB, int KD, int NH = NB / 2>
 __device__ __forceinline__ void accumulate_window(uint32_t taddr, int col0, long long* hi, long long* mid,
                                                   float* lo) {
-    // NH: columns of this thread's part of the row (16, 8 or 4)
+    if constexpr (NH == 16) {
 #pragma unroll
-    for (int g = 0; g < KD; ++g) {
-        float v[NH];
-        if constexpr (NH == 16) tc::tmem_ld16(taddr + (uint32_t)(g * NB + col0), v);
-        else if constexpr (NH == 8) tc::tmem_ld8(taddr + (uint32_t)(g * NB + col0), v);
-        else tc::tmem_ld4(taddr + (uint32_t)(g * NB + col0), v);
-        if (g < 3) {
-            const int sh = 8 * (2 - g);
+        for (int g = 0; g < KD; ++g) {
+            float v[NH];
+            tc::tmem_ld16(taddr + (uint32_t)(g * NB + col0), v);
+            add_group<NH>(g, v, hi, mid, lo);
+        }
+    } else {
+        static_assert(NH == 8 || NH == 4, "columns per thread");
+        constexpr int GB = NH == 8 ? 4 : KD;   // groups per batch of loads (32 or 28 registers)
 #pragma unroll
-            for (int q = 0; q < NH; ++q) hi[q] += (long long)__float2int_rn(v[q]) << sh;
-        } else if (g < 6) {
-            const int sh = 8 * (5 - g);
+        for (int g0 = 0; g0 < KD; g0 += GB) {
+            uint32_t r[GB][NH];
 #pragma unroll
-            for (int q = 0; q < NH; ++q) mid[q] += (long long)__float2int_rn(v[q]) << sh;
-        } else {
-            const float w = __int_as_float((127 - 8 * (g - 6)) << 23);  // 2^{-8(g-6)}
+            for (int b = 0; b < GB; ++b) {
+                if (g0 + b >= KD) break;
+                if constexpr (NH == 8) tc::tmem_ld8_nowait(taddr + (uint32_t)((g0 + b) * NB + col0), r[b]);
+                else tc::tmem_ld4_nowait(taddr + (uint32_t)((g0 + b) * NB + col0), r[b]);
+            }
+            tc::tmem_wait_ld();
 #pragma unroll
-            for (int q = 0; q < NH; ++q) lo[q] = fmaf(v[q], w, lo[q]);
+            for (int b = 0; b < GB; ++b) {
+                if (g0 + b >= KD) break;
+                if constexpr (NH == 8) tc::tmem_tie8(r[b]);
+                else tc::tmem_tie4(r[b]);
+                float v[NH];
+#pragma unroll
+                for (int q = 0; q < NH; ++q) v[q] = __uint_as_float(r[b][q]);
+                add_group<NH>(g0 + b, v, hi, mid, lo);
+            }
         }
     }
 }
@@ -485,23 +524,41 @@ __device__ __forceinline__ void accumulate_window(uint32_t taddr, int col0, long
 // hi = D0 2^16 + D1 2^8 + D2, mid = D3 2^16 + D4 2^8 + D5, lo = D6 + D7 2^-8 + ...,
 // W = 2^64 * sum_g D_g 2^{-8g}.
 __device__ __forceinline__ double assemble(long long hi, long long mid, float lo, int e2) {
-    const __int128 W = ((__int128)hi << 48) + ((__int128)mid << 24) + (__int128)__float2ll_rn(lo * 65536.0f);
-    if (W == 0) return 0.0;
-    const unsigned long long sign = W < 0 ? 0x8000000000000000ULL : 0ULL;
-    const unsigned __int128 A = W < 0 ? (unsigned __int128)(-W) : (unsigned __int128)W;
-    const unsigned long long ah = (unsigned long long)(A >> 64), al = (unsigned long long)A;
-    const int p = ah ? 127 - __clzll((long long)ah) : 63 - __clzll((long long)al);  // leading bit
-    unsigned long long mant;
-    int pe = p;
-    if (p > 52) {
-        const int sh = p - 52;
-        mant = (unsigned long long)(A >> sh);
-        const unsigned long long rbit = (unsigned long long)(A >> (sh - 1)) & 1ULL;
-        mant += rbit;
-        if (mant >> 53) { mant >>= 1; ++pe; }
-    } else {
-        mant = al << (52 - p);
+    // W as two 64-bit limbs (wh, wl): the three terms sign-extended and added with
+    // the carries out of the low limb.
+    const long long L = __float2ll_rn(lo * 65536.0f);
+    unsigned long long wl = (unsigned long long)hi << 48;
+    unsigned long long wh = (unsigned long long)(hi >> 16);
+    const unsigned long long ml = (unsigned long long)mid << 24;
+    unsigned long long t = wl + ml;
+    wh += (unsigned long long)(mid >> 40) + (unsigned long long)(t < wl);
+    wl = t;
+    t = wl + (unsigned long long)L;
+    wh += (unsigned long long)(L >> 63) + (unsigned long long)(t < wl);
+    wl = t;
+    if ((wl | wh) == 0ULL) return 0.0;
+    const unsigned long long sign = wh & 0x8000000000000000ULL;
+    if (sign) {   // |W|
+        wl = ~wl + 1ULL;
+        wh = ~wh + (unsigned long long)(wl == 0ULL);
     }
+    // T: the 64 bits of |W| from its leading one (at bit p) down, the leading one
+    // at bit 63. The 53-bit mantissa is T >> 11, rounded by bit 10 (half away from
+    // zero); below 2^53 T's low bits are zero and nothing rounds.
+    int p;
+    unsigned long long T;
+    if (wh) {
+        const int lz = __clzll((long long)wh);
+        p = 127 - lz;
+        T = lz ? (wh << lz) | (wl >> (64 - lz)) : wh;
+    } else {
+        const int lz = __clzll((long long)wl);
+        p = 63 - lz;
+        T = wl << lz;
+    }
+    unsigned long long mant = (T >> 11) + ((T >> 10) & 1ULL);
+    int pe = p;
+    if (mant >> 53) { mant >>= 1; ++pe; }
     const int E = pe + e2 + 1023;
     if (E <= 0) return __longlong_as_double((long long)sign);
     if (E >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ULL));
@@ -587,9 +644,9 @@ __device__ __forceinline__ Bars* setup_cta(uint8_t* smem_raw, uint8_t*& sA, uint
     if (threadIdx.x == 0) {
         for (int i = 0; i < RA; ++i) { tc::mbar_init(&bars->a_full[i], 1); tc::mbar_init(&bars->a_empty[i], 1); }
         for (int i = 0; i < RB; ++i) { tc::mbar_init(&bars->b_full[i], 1); tc::mbar_init(&bars->b_empty[i], 1); }
-        for (int i = 0; i < 2; ++i) { tc::mbar_init(&bars->t_full[i], 1); tc::mbar_init(&bars->t_empty[i], (uint32_t)nepi); }
+        for (int i = 0; i < 2; ++i) { tc::mbar_init(&bars->t_full[i], 1); tc::mbar_init(&bars->t_empty[i], (uint32_t)(nepi / 32)); }
         tc::mbar_init(&bars->drain, 1);
-        // Tile-number ring: one producer; the MMA thread and the 8 epilogue warps read.
+        // Tile-number ring: one producer; the MMA thread and every epilogue warp read.
         for (int i = 0; i < RQ; ++i) { tc::mbar_init(&bars->q_full[i], 1); tc::mbar_init(&bars->q_empty[i], (uint32_t)(1 + nepi / 32)); }
         tc::fence_mbar_init();
     }
@@ -725,12 +782,15 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
         for (int w = 0; w < nwin; ++w) {
             const int buf = w & 1;
             const uint32_t tph = (uint32_t)((w >> 1) & 1);
-            if (!tc::mbar_wait(&bars->t_full[buf], tph, &abort_flag, p.err, 41)) { ok = false; break; }
+            // Warp-uniform: the TMEM loads below are .sync.aligned.
+            const bool got = tc::mbar_wait(&bars->t_full[buf], tph, &abort_flag, p.err, 41);
+            if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
             tc::tc_fence_after();
             const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * L::TMEM_COLS_PER_BUF);
             accumulate_window<NB, KD>(taddr, half * NH, hi, mid, lo);
             tc::tc_fence_before();
-            tc::mbar_arrive(&bars->t_empty[buf]);
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&bars->t_empty[buf]);   // one arrival per warp
         }
         if (ok && !abort_flag) {
             const int c = mb * TILE_M + row;
@@ -967,14 +1027,17 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
             for (int w = 0; w < nwin; ++w, ++wc) {
                 const int buf = wc & 1;
                 const uint32_t tph = (uint32_t)((wc >> 1) & 1);
-                if (!tc::mbar_wait(&bars->t_full[buf], tph, &abort_flag, p0.err, 42)) { ok = false; break; }
+                // Warp-uniform: the TMEM loads below are .sync.aligned.
+                const bool got = tc::mbar_wait(&bars->t_full[buf], tph, &abort_flag, p0.err, 42);
+                if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
                 tc::tc_fence_after();
                 const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * L::TMEM_COLS_PER_BUF);
                 accumulate_window<NB, KD, NH>(taddr, half * NH, hi, mid, lo);
                 tc::tc_fence_before();
-                tc::mbar_arrive(&bars->t_empty[buf]);
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&bars->t_empty[buf]);   // one arrival per warp
             }
-            if (!ok || abort_flag) break;
+            if (__any_sync(0xffffffffu, !ok || abort_flag)) break;
             const i64 r = (i64)lt * TILE_M + rloc;
             double* xr = q->X + r + (i64)q->c0 * q->ld;
 #pragma unroll
