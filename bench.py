@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--fast-steps", type=int, default=1,
                     help="timed 48-bit split QRs reported beside the 56-bit split run")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-cuda-host-alloc", action="store_true",
+                    help="add an e2e leg on cudaHostAlloc host buffers beside the huge-page ones")
+    ap.add_argument("--e2e-pageable", action="store_true",
+                    help="add an e2e leg on pageable (malloc) host buffers, one sample")
     ap.add_argument("--cpu-rows", type=int, default=1 << 21,
                     help="rows of the bounded CPU sample of the cpu_baseline leg (time scaled to m)")
     ap.add_argument("--ref-budget-s", type=float, default=180.0,
@@ -380,37 +384,59 @@ def run_ours(args, rank, world, local_rank):
         ms_ = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
         return ms_, ({} if args.no_accuracy else accuracy())
 
-    # End to end through the orth.h host entry point (pinned host buffers), right after
-    # the timed region, before the side legs change the GPU's state.
+    # End to end through the orth.h host entry point (page-locked host buffers), right
+    # after the timed region, before the side legs change the GPU's state. The buffers
+    # come from the library's orth_gb300_host_alloc (huge-page backed, registered);
+    # --e2e-cuda-host-alloc adds a leg on cudaHostAlloc memory (torch pin_memory).
     e2e = None
     if not args.no_e2e and args.e2e_steps > 0:
         import numpy as np
-        Xh_t = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
-        Rh_t = torch.zeros((n, n), dtype=torch.float64, pin_memory=True)
-        Xh = Xh_t.numpy().T          # m x n column-major view, ld = m
-        Rh = Rh_t.numpy().T
-        work = np.zeros(1)
+
+        def host_leg(Xh, Rh, samples):
+            Xh_t = torch.from_numpy(Xh.T)      # (n, m) view of the m x n column-major buffer
+            Rh_t = torch.from_numpy(Rh.T)
+            work = np.zeros(1)
+            times, timelines = [], []
+            for k in range(samples + 1):
+                Xh_t.copy_(X0, non_blocking=False)
+                Rh_t.zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                rc = orth.call(variant, m, n, s, Xh, m, Rh, n, work, orth.lwork_min(m, n, s, variant))
+                dt = time.perf_counter() - t0
+                if rc != 0:
+                    raise RuntimeError(f"host entry point rc={rc}")
+                if k > 0:   # first call warms the host-path buffers
+                    times.append(dt * 1e3)
+                    timelines.append(orth.last_host_timing())
+            return times, {key: round(sum(t[key] for t in timelines) / len(timelines), 1) for key in timelines[0]}
+
         orth.set_host_precision(prec)
-        times, timelines = [], []
-        for k in range(args.e2e_steps + 1):
-            Xh_t.copy_(X0, non_blocking=False)
-            Rh_t.zero_()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            rc = orth.call(variant, m, n, s, Xh, m, Rh, n, work, orth.lwork_min(m, n, s, variant))
-            dt = time.perf_counter() - t0
-            if rc != 0:
-                raise RuntimeError(f"host entry point rc={rc}")
-            if k > 0:   # first call warms the host-path buffers
-                times.append(dt * 1e3)
-                timelines.append(orth.last_host_timing())
+        hx, hr = orth.HostBuffer(m * n * 8), orth.HostBuffer(n * n * 8)
+        times, timeline = host_leg(hx.array((m, n)), hr.array((n, n)), args.e2e_steps)
+        hx.close()
+        hr.close()
         e2e_ms = max_over_ranks(sum(times) / len(times), world, dev)
         e2e = {"value": round(e2e_ms, 3), "unit": "ms", "samples_ms": [round(x, 1) for x in times],
-               "timeline_ms": {key: round(sum(t[key] for t in timelines) / len(timelines), 1)
-                               for key in timelines[0]},
+               "timeline_ms": timeline,
                "h2d_bytes_per_step": m * n * 8, "d2h_bytes_per_step": m * n * 8 + n * n * 8,
-               "path": f"orth.h {variant} (host pointers, pinned), {prec_name}"}
-        del Xh_t, Rh_t
+               "path": f"orth.h {variant} (host pointers: page-locked huge-page buffers from "
+                       f"orth_gb300_host_alloc), {prec_name}"}
+        if args.e2e_cuda_host_alloc:
+            Xc = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
+            Rc = torch.zeros((n, n), dtype=torch.float64, pin_memory=True)
+            t2, tl2 = host_leg(Xc.numpy().T, Rc.numpy().T, args.e2e_steps)
+            e2e["cuda_host_alloc"] = {"value": round(sum(t2) / len(t2), 3), "samples_ms": [round(x, 1) for x in t2],
+                                      "timeline_ms": tl2,
+                                      "path": "the same call on cudaHostAlloc buffers (torch pin_memory)"}
+            del Xc, Rc
+        if args.e2e_pageable:
+            Xq = np.zeros((m, n), order="F")
+            Rq = np.zeros((n, n), order="F")
+            t3, tl3 = host_leg(Xq, Rq, 1)
+            e2e["pageable"] = {"value": round(sum(t3) / len(t3), 3), "samples_ms": [round(x, 1) for x in t3],
+                               "timeline_ms": tl3, "path": "the same call on ordinary (pageable) numpy buffers"}
+            del Xq, Rq
 
     # FP64 leg and 48-bit split leg beside the 56-bit split run.
     fp64_ms = fp64_acc = fast_ms = fast_acc = None

@@ -102,6 +102,10 @@ def load(path: str | None = None):
     lib.orth_gb300_set_intra_ortho.restype = ctypes.c_int
     lib.orth_gb300_set_host_precision.argtypes = [ctypes.c_int]
     lib.orth_gb300_set_host_precision.restype = ctypes.c_int
+    lib.orth_gb300_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
+    lib.orth_gb300_host_alloc.restype = ctypes.c_int
+    lib.orth_gb300_host_free.argtypes = [ctypes.c_void_p]
+    lib.orth_gb300_host_free.restype = ctypes.c_int
     lib.orth_gb300_last_split_error.argtypes = []
     lib.orth_gb300_last_split_error.restype = ctypes.c_int
     lib.orth_gb300_split_supported.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -211,6 +215,45 @@ def timeout_probe(code: int, stream: int = 0):
     out = (ctypes.c_int * 2)()
     rc = int(load().orth_gb300_timeout_probe(code, ctypes.c_void_p(stream), out))
     return rc, out[0], out[1]
+
+
+class HostBuffer:
+    """Page-locked, huge-page-backed host memory from orth_gb300_host_alloc.
+
+    ``array(shape, order)`` gives a float64 numpy view of it (zero-filled at
+    allocation). The buffer is released by ``close()`` or when the object is
+    collected; views must not outlive it.
+    """
+
+    def __init__(self, nbytes: int):
+        self.nbytes = int(nbytes)
+        self._p = ctypes.c_void_p(0)
+        rc = int(load().orth_gb300_host_alloc(ctypes.c_size_t(self.nbytes), ctypes.byref(self._p)))
+        if rc != 0:
+            raise RuntimeError(f"orth_gb300_host_alloc({self.nbytes}) returned {rc}")
+
+    @property
+    def ptr(self) -> int:
+        return int(self._p.value or 0)
+
+    def array(self, shape, order: str = "F"):
+        import numpy as np
+        count = int(np.prod(shape))
+        if count * 8 > self.nbytes:
+            raise ValueError("shape exceeds the buffer")
+        flat = np.ctypeslib.as_array((ctypes.c_double * count).from_address(self.ptr))
+        return flat.reshape(shape, order=order)
+
+    def close(self) -> None:
+        if self._p.value:
+            load().orth_gb300_host_free(self._p)
+            self._p = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def last_host_timing() -> dict:

@@ -6,12 +6,15 @@
 // deterministic device-wide reduction and every small s x s step kept on the
 // device, so a whole QR is enqueued on one stream with no host round trip.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <climits>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/orth.h"
@@ -244,10 +247,20 @@ int reserve(i64 m, int n, int s, int precision) {
 // ---------------------------------------------------------------------------
 // Host-buffer runs (the orth.h entry points): X arrives in column chunks on one
 // copy stream and Q leaves on another while the QR runs; the two directions
-// overlap on the link. The compute stream waits
-// only for the chunks a primitive reads (need). Every update or TSQR that writes
-// from column c0 marks columns [0, c0) final (final). No variant writes a column
-// left of the block it is working on, so those columns can be copied back at once.
+// overlap on the link. The compute stream waits only for the chunks a primitive
+// reads (need). Every update or TSQR that writes from column c0 marks columns
+// [0, c0) final (final). No variant writes a column left of the block it is
+// working on, so those columns can be copied back at once.
+//
+// Page-locked host buffers take asynchronous copies issued from the calling
+// thread. A copy to or from pageable memory returns only once the driver has
+// taken the data (to the device) or delivered it (to the host), so issued from
+// the calling thread it would hold back the launches behind it: the QR would
+// wait for each chunk of Q to reach the host. For a pageable X the copies are
+// issued by two worker threads instead (uploader, downloader) on the same copy
+// streams; need() then waits on the host until the uploader has issued the
+// chunk's copy and recorded its event, and final() hands the downloader an
+// event recorded on the compute stream.
 // ---------------------------------------------------------------------------
 struct HostLink {
     double* hX = nullptr;   // caller's X (host), ld ldh
@@ -255,9 +268,23 @@ struct HostLink {
     int n = 0, chunk = 1;
     double* dX = nullptr;   // device copy, ld m
     cudaStream_t cin = nullptr, cout = nullptr;
-    std::vector<cudaEvent_t> ev_in;
+    bool pageable = false;           // hX is not page-locked: copies go through the worker threads
+    cudaEvent_t x_done = nullptr;    // recorded on cin after the last chunk of X (if set)
+    std::vector<cudaEvent_t> ev_in;  // one per chunk of X, recorded on cin after its copy
+    std::vector<cudaEvent_t> ev_out; // final() events (pageable path)
     cudaEvent_t ev_fin = nullptr;
-    int waited = 0, out_done = 0, err = 0;
+    int waited = 0, out_done = 0;
+    std::atomic<int> err{0};
+    int dev = 0;
+
+    // Worker threads (pageable path).
+    struct Req { cudaEvent_t ev; int c0, c1; };
+    std::thread up, down;
+    std::mutex mu;
+    std::condition_variable cv;
+    int issued_in = 0;               // chunks whose copy is issued and event recorded
+    std::vector<Req> reqs;           // final() requests not yet taken by the downloader
+    bool closing = false;
 
     cudaError_t copy(double* dst, i64 ldd, const double* src, i64 lds, int c0, int nc, cudaMemcpyKind kind,
                      cudaStream_t s) {
@@ -267,42 +294,119 @@ struct HostLink {
         return cudaMemcpy2DAsync(dst + (i64)c0 * ldd, (size_t)ldd * sizeof(double), src + (i64)c0 * lds,
                                  (size_t)lds * sizeof(double), w, (size_t)nc, kind, s);
     }
+    void fail(int e) {
+        int z = 0;
+        err.compare_exchange_strong(z, e);
+    }
+    // Issue chunk k of X and record its event (either thread).
+    int put_chunk(int k) {
+        const int c0 = k * chunk;
+        const int nc = n - c0 < chunk ? n - c0 : chunk;
+        int e = (int)copy(dX, m, hX, ldh, c0, nc, cudaMemcpyHostToDevice, cin);
+        if (!e) e = (int)cudaEventRecord(ev_in[k], cin);
+        return e;
+    }
     // Enqueue every H2D chunk on cin (after `st` reaches this point).
     void start(cudaStream_t st) {
+        (void)cudaGetDevice(&dev);
         cudaEvent_t e0 = nullptr;
-        if ((err = (int)cudaEventCreateWithFlags(&e0, cudaEventDisableTiming))) return;
+        int e = (int)cudaEventCreateWithFlags(&e0, cudaEventDisableTiming);
+        if (e) { fail(e); return; }
         cudaEventRecord(e0, st);
         cudaStreamWaitEvent(cin, e0, 0);
         cudaStreamWaitEvent(cout, e0, 0);
         cudaEventDestroy(e0);
-        if ((err = (int)cudaEventCreateWithFlags(&ev_fin, cudaEventDisableTiming))) return;
-        for (int c0 = 0; c0 < n && !err; c0 += chunk) {
-            const int nc = n - c0 < chunk ? n - c0 : chunk;
-            cudaEvent_t e = nullptr;
-            if ((err = (int)cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) break;
-            ev_in.push_back(e);
-            if ((err = (int)copy(dX, m, hX, ldh, c0, nc, cudaMemcpyHostToDevice, cin))) break;
-            err = (int)cudaEventRecord(e, cin);
+        if ((e = (int)cudaEventCreateWithFlags(&ev_fin, cudaEventDisableTiming))) { fail(e); return; }
+        const int nchunks = (n + chunk - 1) / chunk;
+        for (int k = 0; k < nchunks; ++k) {
+            cudaEvent_t ek = nullptr;
+            if ((e = (int)cudaEventCreateWithFlags(&ek, cudaEventDisableTiming))) { fail(e); return; }
+            ev_in.push_back(ek);
         }
+        if (!pageable) {
+            for (int k = 0; k < nchunks && !err; ++k)
+                if ((e = put_chunk(k))) fail(e);
+            if (!err && x_done && (e = (int)cudaEventRecord(x_done, cin))) fail(e);
+            issued_in = nchunks;
+            return;
+        }
+        up = std::thread([this, nchunks] {
+            int e = (int)cudaSetDevice(dev);
+            for (int k = 0; k < nchunks; ++k) {
+                if (!e && !err) e = put_chunk(k);
+                if (e) fail(e);
+                std::lock_guard<std::mutex> lock(mu);
+                issued_in = k + 1;
+                cv.notify_all();
+            }
+            if (!err && x_done && (e = (int)cudaEventRecord(x_done, cin))) fail(e);
+        });
     }
     void need(cudaStream_t st, int c_end) {
         while (!err && waited < c_end && waited < n) {
-            err = (int)cudaStreamWaitEvent(st, ev_in[waited / chunk], 0);
-            waited = (waited / chunk + 1) * chunk;
+            const int k = waited / chunk;
+            if (pageable) {
+                std::unique_lock<std::mutex> lock(mu);
+                cv.wait(lock, [&] { return issued_in > k || err != 0; });
+                if (err) break;
+            }
+            const int e = (int)cudaStreamWaitEvent(st, ev_in[k], 0);
+            if (e) fail(e);
+            waited = (k + 1) * chunk;
         }
     }
     void final(cudaStream_t st, int c_end) {
         if (err || c_end <= out_done) return;
         if (c_end > n) c_end = n;
-        err = (int)cudaEventRecord(ev_fin, st);
-        if (!err) err = (int)cudaStreamWaitEvent(cout, ev_fin, 0);
-        if (!err) err = (int)copy(hX, ldh, dX, m, out_done, c_end - out_done, cudaMemcpyDeviceToHost, cout);
+        int e = 0;
+        if (!pageable) {
+            e = (int)cudaEventRecord(ev_fin, st);
+            if (!e) e = (int)cudaStreamWaitEvent(cout, ev_fin, 0);
+            if (!e) e = (int)copy(hX, ldh, dX, m, out_done, c_end - out_done, cudaMemcpyDeviceToHost, cout);
+            if (e) fail(e);
+            out_done = c_end;
+            return;
+        }
+        cudaEvent_t ev = nullptr;
+        e = (int)cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (!e) e = (int)cudaEventRecord(ev, st);
+        if (e) {
+            if (ev) cudaEventDestroy(ev);
+            fail(e);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            ev_out.push_back(ev);
+            reqs.push_back(Req{ev, out_done, c_end});
+            cv.notify_all();
+        }
         out_done = c_end;
+        if (!down.joinable()) {
+            down = std::thread([this] {
+                int e = (int)cudaSetDevice(dev);
+                if (e) fail(e);
+                for (;;) {
+                    Req r;
+                    {
+                        std::unique_lock<std::mutex> lock(mu);
+                        cv.wait(lock, [&] { return !reqs.empty() || closing; });
+                        if (reqs.empty()) return;
+                        r = reqs.front();
+                        reqs.erase(reqs.begin());
+                    }
+                    if (err) continue;   // drain the queue without copying
+                    e = (int)cudaStreamWaitEvent(cout, r.ev, 0);
+                    if (!e) e = (int)copy(hX, ldh, dX, m, r.c0, r.c1 - r.c0, cudaMemcpyDeviceToHost, cout);
+                    if (e) fail(e);
+                }
+            });
+        }
     }
     // The last columns of Q and all of R, enqueued before the caller reads the run's
     // status, so that they do not wait for that read. R goes to the staging buffer
-    // hR on the compute stream; done (if set) is recorded there when the QR's
-    // kernels have finished, before R's copy.
+    // hR (page-locked) on the compute stream; done (if set) is recorded there when
+    // the QR's kernels have finished, before R's copy.
     double* hR = nullptr;
     const double* dR = nullptr;
     size_t rbytes = 0;
@@ -310,16 +414,32 @@ struct HostLink {
     bool finished = false;
     void finish(cudaStream_t st) {
         final(st, n);
-        if (!err && done) err = (int)cudaEventRecord(done, st);
-        if (!err) err = (int)cudaMemcpyAsync(hR, dR, rbytes, cudaMemcpyDeviceToHost, st);
+        int e = 0;
+        if (!err && done && (e = (int)cudaEventRecord(done, st))) fail(e);
+        if (!err && (e = (int)cudaMemcpyAsync(hR, dR, rbytes, cudaMemcpyDeviceToHost, st))) fail(e);
         finished = !err;
     }
+    // Waits for the worker threads: after it returns every copy of this run is
+    // issued (and, for pageable memory, complete).
+    void join() {
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            closing = true;
+            cv.notify_all();
+        }
+        if (up.joinable()) up.join();
+        if (down.joinable()) down.join();
+    }
     void release() {
+        join();
         for (cudaEvent_t e : ev_in) cudaEventDestroy(e);
         ev_in.clear();
+        for (cudaEvent_t e : ev_out) cudaEventDestroy(e);
+        ev_out.clear();
         if (ev_fin) cudaEventDestroy(ev_fin);
         ev_fin = nullptr;
     }
+    ~HostLink() { join(); }
 };
 
 // ---------------------------------------------------------------------------
@@ -922,6 +1042,16 @@ bool is_device_pointer(const void* p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Page-locked host memory (cudaHostAlloc, cudaHostRegister, orth_gb300_host_alloc).
+bool is_page_locked(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 // Copies what the reference writes into R (SRC/orth.c): for column j of block b,
 // rows [0, end of block b); bcgsi21s writes only the upper triangle of its
 // diagonal blocks after the first (SRC/orth.c:302,360 use dlacpy 'U').
@@ -1008,6 +1138,7 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
     link.hX = Xsub; link.ldh = ldXsub; link.m = m; link.n = n; link.dX = dX;
     link.cin = g_ctx.copy_in; link.cout = g_ctx.copy_out;
     link.hR = g_ctx.hostR_stage; link.dR = dR; link.rbytes = rbytes;
+    link.pageable = !is_page_locked(Xsub);
     {
         const i64 per64mb = ((i64)64 << 20) / ((i64)m * (i64)sizeof(double));
         link.chunk = (int)(per64mb > s ? (per64mb < n ? per64mb : n) : s);
@@ -1017,16 +1148,17 @@ int run_host(int variant, int m, int n, int s, double* Xsub, int ldXsub, double*
     bool timed = false;
     cudaError_t ce = cudaEventRecord(tev[0], st);
     if (ce == cudaSuccess) ce = (cudaError_t)zero_async(dR, rbytes, st);
+    link.x_done = tev[1];
     if (ce == cudaSuccess) {
         link.start(st);
-        ce = (cudaError_t)link.err;
-        if (ce == cudaSuccess) ce = cudaEventRecord(tev[1], g_ctx.copy_in);
+        ce = (cudaError_t)link.err.load();
     }
     link.done = tev[2];
     if (ce == cudaSuccess) {
         rc = run_device(variant, m, n, s, dX, m, dR, n, precision, st, &stt, &link);
+        link.join();   // every copy issued (pageable: complete)
         if (!rc) {
-            ce = link.finished ? (cudaError_t)link.err : cudaErrorUnknown;
+            ce = link.finished ? (cudaError_t)link.err.load() : cudaErrorUnknown;
             if (ce == cudaSuccess) ce = cudaEventRecord(tev[3], g_ctx.copy_out);
             timed = ce == cudaSuccess;
         }

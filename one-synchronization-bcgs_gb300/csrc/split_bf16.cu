@@ -127,11 +127,30 @@ __device__ __forceinline__ void colmax_body(const double* __restrict__ X, i64 ld
                                             unsigned long long* __restrict__ cmax) {
     const i64 r0 = (i64)rb * 4096;
     const i64 r1 = min(m, r0 + 4096);
+    const double* col = X + (i64)c * ld;
+    // 4096 rows over the CTA's threads, all loads of a thread issued before any
+    // is used (16 in flight per thread at 256 threads).
+    constexpr int kMaxIt = 16;
     unsigned long long v = 0;
-    for (i64 r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        unsigned long long b = (unsigned long long)__double_as_longlong(X[r + (i64)c * ld]) & 0x7FFFFFFFFFFFFFFFULL;
-        if ((b >> 52) == 0x7FF) b = 0;  // Inf/NaN do not set the scale
-        v = v > b ? v : b;
+    const int step = (int)blockDim.x;
+    if (r0 + (i64)step * kMaxIt >= r1) {
+        unsigned long long b[kMaxIt];
+#pragma unroll
+        for (int k = 0; k < kMaxIt; ++k) {
+            const i64 r = r0 + threadIdx.x + (i64)k * step;
+            b[k] = r < r1 ? ((unsigned long long)__double_as_longlong(col[r]) & 0x7FFFFFFFFFFFFFFFULL) : 0ULL;
+        }
+#pragma unroll
+        for (int k = 0; k < kMaxIt; ++k) {
+            const unsigned long long bk = (b[k] >> 52) == 0x7FF ? 0ULL : b[k];   // Inf/NaN do not set the scale
+            v = v > bk ? v : bk;
+        }
+    } else {
+        for (i64 r = r0 + threadIdx.x; r < r1; r += step) {
+            unsigned long long b = (unsigned long long)__double_as_longlong(col[r]) & 0x7FFFFFFFFFFFFFFFULL;
+            if ((b >> 52) == 0x7FF) b = 0;
+            v = v > b ? v : b;
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {

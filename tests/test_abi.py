@@ -90,3 +90,13 @@ def test_split_shape_support(lib):
 def test_timeout_probe_rejects_code_zero(lib):
     # Code 0 means "no error" and is rejected before any CUDA call.
     assert orth.timeout_probe(0)[0] == 2
+
+
+def test_host_buffer_argument_checks(lib):
+    """orth_gb300_host_alloc / _free reject bad arguments before any CUDA call."""
+    import ctypes
+    p = ctypes.c_void_p(0)
+    assert lib.orth_gb300_host_alloc(ctypes.c_size_t(0), ctypes.byref(p)) == 2 and not p.value
+    assert lib.orth_gb300_host_alloc(ctypes.c_size_t(64), None) == 2
+    assert lib.orth_gb300_host_free(None) == 0
+    assert lib.orth_gb300_host_free(ctypes.c_void_p(0x12345000)) == 2   # not from orth_gb300_host_alloc
