@@ -23,7 +23,14 @@ typedef struct orth_gb300_status {
     int cuda_error;      /* cudaError_t of the first failing CUDA call, 0 if none */
 } orth_gb300_status;
 
-/* Precision modes of the tall products (Q^T V and Q S). */
+/*
+ * Precision modes of the tall products (Q^T V and Q S). The split modes hold each
+ * column as fixed point scaled by the column's maximum, so entries far below
+ * their column's maximum keep fewer significant bits than in FP64. The
+ * environment variable ORTH_GB300_SPLIT_GRAM_PLANES=6 makes the 56-bit mode's Gram
+ * read 6 planes of its first operand (faster, less accurate for columns
+ * dominated by a few rows); the default reads all 7.
+ */
 #define ORTH_GB300_FP64 0             /* plain FP64 on the FP64 pipe */
 #define ORTH_GB300_SPLIT_BF16 1       /* tensor cores, 7 BF16 digit planes (56-bit fixed point) */
 #define ORTH_GB300_SPLIT_BF16_FAST 2  /* tensor cores, 6 BF16 digit planes (48-bit fixed point) */

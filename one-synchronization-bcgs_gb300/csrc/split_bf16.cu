@@ -61,7 +61,8 @@ namespace {
 constexpr int KD_MAX = 7;      // digit planes held by the stores
 constexpr int TILE_M = 128;    // MMA M (rows of D = TMEM lanes)
 constexpr int KCH = 64;        // K elements per chunk (one 128-byte swizzle row)
-constexpr int WIN = 4;         // chunks per accumulation window (256 summation steps)
+constexpr int WIN = 2;         // chunks per accumulation window (128 summation steps)
+constexpr int ROW_ALIGN = 256; // Gram row ranges: multiples of 256 rows (whole windows)
 constexpr int RA = 8;          // A ring depth (16 KB slots)
 constexpr int RB = 2;          // B ring depth
 constexpr int A_SLOT = TILE_M * KCH * 2;   // 16 KB
@@ -495,8 +496,9 @@ __device__ __forceinline__ void add_group(int g, const float* v, long long* hi, 
 // Per-window epilogue accumulation of the TMEM groups: groups 0-2 (weights 1,
 // 2^-8, 2^-16) into the exact 64-bit integer hi, groups 3-5 into the exact 64-bit
 // integer mid (weight 2^-24 relative to hi's unit), and groups >= 6 (weight <=
-// 2^-48) into FP32. Each TMEM value is an integer below 2^24.6 (at most 3 products
-// of |digit| <= 2^7 per summation step, 256 steps per window). With 8 or 4
+// 2^-48) into FP32. Group g sums g + 1 digit products of magnitude <= 2^14 per
+// summation step; over the 128 steps of a window every partial sum of every group
+// stays below 7 * 2^21 < 2^24, so the FP32 accumulation in TMEM is exact. With 8 or 4
 // columns per thread the group loads go out in batches (4 groups, or all) under
 // one wait each; with 16 (the Gram, not bound by its epilogue) each load waits
 // on its own.
@@ -584,11 +586,11 @@ __device__ __forceinline__ double assemble(long long hi, long long mid, float lo
     return __longlong_as_double((long long)(sign | ((unsigned long long)E << 52) | (mant & 0xFFFFFFFFFFFFFULL)));
 }
 
-// Producer: for each chunk, B planes then KD A planes (TMA), each with its L2
-// eviction policy (polA, polB). The coordinate function also picks the A map
+// Producer: for each chunk, KD B planes then the KA most significant A planes
+// (TMA), each with its L2 eviction policy (polA, polB). The coordinate function also picks the A map
 // and the bytes its box holds: the update's last K chunk uses a map whose box
 // covers only the chunk's valid columns, so it does not read past kin.
-template <int NB, int KD, class CoordFn>
+template <int NB, int KD, int KA = KD, class CoordFn>
 __device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapB, uint8_t* sA, uint8_t* sB, Bars* bars,
                                               Ring& ra, Ring& rb, CoordFn coords, int item, int ch,
                                               volatile int* abort, int* err, uint64_t polA, uint64_t polB) {
@@ -606,7 +608,7 @@ __device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapB, uint8_t* 
                              bz + j * bzs, polB);
     rb.advance(RB);
 #pragma unroll
-    for (int i = 0; i < KD; ++i) {
+    for (int i = 0; i < KA; ++i) {
         if (!tc::mbar_wait(&bars->a_empty[ra.slot], ra.phase ^ 1u, abort, err, 12 + 100 * ra.slot)) return false;
         tc::mbar_expect_tx(&bars->a_full[ra.slot], abytes);
         tc::tma_load_3d_hint(sA + ra.slot * A_SLOT, mapA, &bars->a_full[ra.slot], ax, ay, az + i * azs, polA);
@@ -615,11 +617,12 @@ __device__ __forceinline__ bool produce_chunk(const CUtensorMap* mapB, uint8_t* 
     return true;
 }
 
-// MMA issuer for one chunk into TMEM buffer `dcol` (column offset). A_MN: the A
+// MMA issuer for one chunk into TMEM buffer `dcol` (column offset): A plane i
+// (i < KA) times B planes 0 .. KD-1-i into TMEM groups i .. KD-1. A_MN: the A
 // tile is two 64-row blocks (LBO apart: 8 KB for a whole chunk, kv * 128 bytes
 // for a last chunk of kv columns) of K-rows of 128 bytes (MN-major); only the
 // first ksteps 16-row K steps are issued.
-template <int NB, int KD, bool A_MN = false>
+template <int NB, int KD, bool A_MN = false, int KA = KD>
 __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uint8_t* sA, uint8_t* sB,
                                           Bars* bars, Ring& ra, Ring& rb, bool first_in_window,
                                           volatile int* abort, int* err, int ksteps = KCH / 16,
@@ -628,7 +631,7 @@ __device__ __forceinline__ bool mma_chunk(uint32_t tmem_base, uint32_t dcol, uin
     if (!tc::mbar_wait(&bars->b_full[rb.slot], rb.phase, abort, err, 21)) return false;
     const uint32_t b_addr = tc::smem_u32(sB + rb.slot * B_SLOT);
 #pragma unroll
-    for (int i = 0; i < KD; ++i) {
+    for (int i = 0; i < KA; ++i) {
         if (!tc::mbar_wait(&bars->a_full[ra.slot], ra.phase, abort, err, 22 + 100 * ra.slot)) return false;
         tc::tc_fence_after();
         const uint32_t a_addr = tc::smem_u32(sA + ra.slot * A_SLOT);
@@ -686,7 +689,7 @@ struct GramParams {
     int alast;       // columns the last M-block's A box holds (na - 128 (numMB - 1), rounded up to 16)
     i64 m;
     int numMB, numNG, rc;
-    i64 rows_per;   // multiple of WIN*KCH
+    i64 rows_per;   // multiple of ROW_ALIGN
     const int* cexp;
     double* part;
     int* err;
@@ -701,7 +704,7 @@ struct SplitGramJob {   // the CUtensorMap members keep the struct 64-byte align
 // BATCH: the CTAs of many Grams in one launch; CTA b runs item b - prefix[j] of
 // job j (prefix[j] <= b < prefix[j + 1]) with job j's maps and parameters, and
 // exactly the arithmetic of a single launch of that Gram. p0.err is the launch's.
-template <int KD, bool BATCH>
+template <int KD, int KA, bool BATCH>
 __global__ void __launch_bounds__(NTHREADS, 1)
 gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapAlast,
                const __grid_constant__ CUtensorMap mapB, GramParams p0, const SplitGramJob* __restrict__ jobs,
@@ -761,8 +764,8 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
             const uint64_t polB = tc::policy_evict_last();
             Ring ra, rb;
             for (int ch = 0; ch < nchunks; ++ch)
-                if (!produce_chunk<NB, KD>(mB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag, p.err, polA,
-                                           polB))
+                if (!produce_chunk<NB, KD, KA>(mB, sA, sB, bars, ra, rb, coords, 0, ch, &abort_flag, p.err, polA,
+                                               polB))
                     break;
             if (abort_flag) {
                 drain_ring(bars->a_full, RA, ra);
@@ -780,8 +783,8 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
                 tc::tc_fence_after();
                 const int c_end = min(nchunks, (w + 1) * WIN);
                 for (int ch = w * WIN; ch < c_end && ok; ++ch)
-                    ok = mma_chunk<NB, KD>(tmem, (uint32_t)(buf * L::TMEM_COLS_PER_BUF), sA, sB, bars, ra, rb,
-                                       ch == w * WIN, &abort_flag, p.err);
+                    ok = mma_chunk<NB, KD, false, KA>(tmem, (uint32_t)(buf * L::TMEM_COLS_PER_BUF), sA, sB, bars, ra,
+                                                      rb, ch == w * WIN, &abort_flag, p.err);
                 if (ok) tc::mma_commit(&bars->t_full[buf]);
             }
             tc::mma_commit(&bars->drain);
@@ -1131,6 +1134,18 @@ int make_map3(CUtensorMap* map, void* base, i64 inner, i64 outer, i64 planes, i6
 
 i64 round_up(i64 a, i64 b) { return (a + b - 1) / b * b; }
 
+// Digit planes of the Gram's first operand. The 56-bit form reads all 7 by
+// default; ORTH_GB300_SPLIT_GRAM_PLANES=6 makes its Gram read the 6 most
+// significant planes of A (B keeps 7): 1/7 fewer A bytes, with A rounded to 48
+// bits in the Gram only (the updates keep 56).
+int gram_a_planes(int kd) {
+    static const int env = [] {
+        const char* v = std::getenv("ORTH_GB300_SPLIT_GRAM_PLANES");
+        return v ? std::atoi(v) : 0;
+    }();
+    return (kd == 7 && env == 6) ? 6 : kd;
+}
+
 struct Plan {
     // geometry
     double* X = nullptr;
@@ -1292,8 +1307,9 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
     if (rc) return rc;
     // Shared-memory limits of the tensor-core kernels on this device.
-    rc = set_smem(gram_tc_kernel<6, false>, SmemLayout<32, 6>::BYTES);
-    if (!rc) rc = set_smem(gram_tc_kernel<7, false>, SmemLayout<32, 7>::BYTES);
+    rc = set_smem(gram_tc_kernel<6, 6, false>, SmemLayout<32, 6>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<7, 7, false>, SmemLayout<32, 7>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<7, 6, false>, SmemLayout<32, 7>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<16, 6, false>, SmemLayout<16, 6>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<16, 7, false>, SmemLayout<16, 7>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<32, 6, false>, SmemLayout<32, 6>::BYTES);
@@ -1350,7 +1366,7 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     gp.numNG = (int)ceil_div(nb, 32);
     const int mbn = gp.numMB * gp.numNG;
     gp.rc = num_sms / mbn > 0 ? num_sms / mbn : 1;
-    gp.rows_per = round_up(ceil_div(m, gp.rc), (i64)WIN * KCH);
+    gp.rows_per = round_up(ceil_div(m, gp.rc), (i64)ROW_ALIGN);
     gp.rc = (int)ceil_div(m, gp.rows_per);
     gp.nrc = (int)P.nrc;
     gp.cexp = P.cexp;
@@ -1366,11 +1382,14 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     const unsigned grid = (unsigned)(mbn * gp.rc);
     const int smem = P.kd == 6 ? SmemLayout<32, 6>::BYTES : SmemLayout<32, 7>::BYTES;
     if (P.kd == 6)
-        gram_tc_kernel<6, false><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp, nullptr,
-                                                               nullptr, 0);
+        gram_tc_kernel<6, 6, false><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp, nullptr,
+                                                                  nullptr, 0);
+    else if (gram_a_planes(P.kd) == 6)
+        gram_tc_kernel<7, 6, false><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp, nullptr,
+                                                                  nullptr, 0);
     else
-        gram_tc_kernel<7, false><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp, nullptr,
-                                                               nullptr, 0);
+        gram_tc_kernel<7, 7, false><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp, nullptr,
+                                                                  nullptr, 0);
     g_launch_count += 1;
     rc = (int)cudaGetLastError();
     if (rc) return rc;
@@ -1754,7 +1773,7 @@ int plan_wave(SplitStaged& S, SWave& W) {
         gp.numNG = (int)ceil_div(nb, 32);
         const int mbn = gp.numMB * gp.numNG;
         gp.rc = S.num_sms / mbn > 0 ? S.num_sms / mbn : 1;
-        gp.rows_per = round_up(ceil_div(P.m, gp.rc), (i64)WIN * KCH);
+        gp.rows_per = round_up(ceil_div(P.m, gp.rc), (i64)ROW_ALIGN);
         gp.rc = (int)ceil_div(P.m, gp.rows_per);
         gp.nrc = (int)P.nrc;
         gp.cexp = P.cexp;
@@ -2109,11 +2128,14 @@ int enqueue_wave(SplitStaged& S, SWave& W, cudaStream_t st) {
             case kSGram: {
                 const auto* J = reinterpret_cast<const SplitGramJob*>(jb + L.job_off);
                 if (KD == 6)
-                    gram_tc_kernel<6, true><<<items, NTHREADS, SmemLayout<32, 6>::BYTES, st>>>(none, none, none, g0, J,
-                                                                                             pre, L.njobs);
+                    gram_tc_kernel<6, 6, true><<<items, NTHREADS, SmemLayout<32, 6>::BYTES, st>>>(
+                        none, none, none, g0, J, pre, L.njobs);
+                else if (gram_a_planes(KD) == 6)
+                    gram_tc_kernel<7, 6, true><<<items, NTHREADS, SmemLayout<32, 7>::BYTES, st>>>(
+                        none, none, none, g0, J, pre, L.njobs);
                 else
-                    gram_tc_kernel<7, true><<<items, NTHREADS, SmemLayout<32, 7>::BYTES, st>>>(none, none, none, g0, J,
-                                                                                             pre, L.njobs);
+                    gram_tc_kernel<7, 7, true><<<items, NTHREADS, SmemLayout<32, 7>::BYTES, st>>>(
+                        none, none, none, g0, J, pre, L.njobs);
                 ++g_launch_count;
                 break;
             }
@@ -2246,8 +2268,9 @@ int split_staged_create(int count, const int* m, const int* n, const int* s, dou
     int rc = fill_smats(*S, count, m, n, s, dX, ldX, dR, ldR, dstatus);
     if (rc) { free_staged(S); return rc; }
     // Shared-memory limits of the batched kernels on this device.
-    rc = set_smem(gram_tc_kernel<6, true>, SmemLayout<32, 6>::BYTES);
-    if (!rc) rc = set_smem(gram_tc_kernel<7, true>, SmemLayout<32, 7>::BYTES);
+    rc = set_smem(gram_tc_kernel<6, 6, true>, SmemLayout<32, 6>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<7, 7, true>, SmemLayout<32, 7>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<7, 6, true>, SmemLayout<32, 7>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<32, 6, true>, SmemLayout<32, 6>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<32, 7, true>, SmemLayout<32, 7>::BYTES);
     if (!rc) rc = set_smem(bbuild_batched, (int)kBbuildSmem);

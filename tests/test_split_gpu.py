@@ -119,3 +119,32 @@ def test_split_wide_blocks(lib, variant, s):
     (Q, R), (Qf, Rf) = out[orth.SPLIT_BF16], out[orth.FP64]
     assert port.loo_2(Q) <= 10 * max(port.loo_2(Qf), 1e-15)
     assert port.rel_residual(X, Q, np.triu(R)) <= 10 * max(port.rel_residual(X, Qf, np.triu(Rf)), 1e-15)
+
+
+@pytest.mark.parametrize("variant", ["bcgsi2P1s", "bcgsi21s", "bcgsi2"])
+@pytest.mark.parametrize("spike", [1e3, 1e6])
+def test_split_spiky_rows(lib, variant, spike):
+    """Columns dominated by a few rows (a graded X whose first 64 rows are scaled by
+    `spike`). The digit planes are fixed point scaled by each column's maximum, so
+    the other rows keep fewer significant bits: the 56-bit form's residual rises
+    to about 3-5e-14 here (measured 2.6e-14 to 5.1e-14 at spike 1e3 and 1e6, the
+    FP64 path below 1e-15), while its orthogonality stays within 10x of FP64's.
+    Checked: the same breakdown step as FP64, LOO_2 within 10x of FP64's, and the
+    residual within the split form's accuracy target (1e-12)."""
+    torch = pytest.importorskip("torch")
+    m, n, s = 200000, 96, 16
+    X = inputs.graded_host(m, n, 1e4, seed=17)
+    X[:64, :] *= spike
+    st = torch.cuda.current_stream().cuda_stream
+    out = {}
+    for prec in (orth.FP64, orth.SPLIT_BF16):
+        dX = _dev(torch, X)
+        dR = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        rc, status = orth.run_dev(variant, m, n, s, dX.data_ptr(), m, dR.data_ptr(), n, prec, st)
+        assert rc == 0 and status["timeout"] == 0, (rc, status)
+        out[prec] = (status["breakdown_step"], dX.cpu().numpy().T.copy(), dR.cpu().numpy().T.copy())
+    (bs, Q, R), (bf, Qf, Rf) = out[orth.SPLIT_BF16], out[orth.FP64]
+    assert bs == bf, (bs, bf)
+    if bf == 0:
+        assert port.loo_2(Q) <= 10 * max(port.loo_2(Qf), 1e-15), (port.loo_2(Q), port.loo_2(Qf))
+        assert port.rel_residual(X, Q, np.triu(R)) <= 1e-12
