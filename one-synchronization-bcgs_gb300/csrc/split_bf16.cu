@@ -10,9 +10,11 @@
 // 2^{2-8(i+j)} are summed in the same TMEM columns: A-plane i is multiplied with the
 // concatenation [B_1 .. B_{KD+1-i}] (N = NB*(KD+1-i)) into TMEM column block i-1,
 // so block g-2 accumulates every product with i + j = g (products with i + j > KD+1
-// are below 2^{-8 KD} and dropped). Groups g = 2..7 are kept exact by emptying the
-// accumulator every 256 summation steps into two 64-bit integers; group g = 8
-// (weight 2^-48 relative) is summed in FP32.
+// are below 2^{-8 KD} and dropped). Block g-2 sums at most g-1 <= 7 products of
+// magnitude <= 2^14 per summation step; the accumulators are emptied every 128
+// summation steps, so every partial sum stays below 7 * 2^21 < 2^24 and the FP32
+// accumulation is exact. Groups g = 2..7 are drained into two exact 64-bit
+// integers; group g = 8 (weight 2^-48 relative) is summed in FP32.
 //
 // One digit store serves both product shapes. It is chunked so that every TMA
 // tile is one contiguous block of HBM:
