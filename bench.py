@@ -252,8 +252,8 @@ def run_reference(args, rank, world):
     oracle restatement (pinned to that build by the tests) runs here with
     OpenBLAS on every host thread. Each timed step is one full-size QR (about
     46 s on 16 Grace cores at m = 2^23), so the steps run are bounded by
-    --ref-budget-s: the line reports how many ran. The warm-up is one QR of a
-    2^16-row sample (thread pools, first-touch of the library)."""
+    --ref-budget-s: the line reports how many ran. Each warm-up step is one QR of
+    a 2^16-row sample (thread pools, first-touch of the library)."""
     if rank != 0:
         return
     m, n, s = args.m, args.n, args.s
@@ -263,8 +263,9 @@ def run_reference(args, rank, world):
     warm = 0
     if args.warmup > 0:
         Xs = X0[: min(m, 1 << 16), :].copy(order="F")
-        port_step(args.variant, Xs, n, s)
-        warm = 1
+        for _ in range(args.warmup):
+            port_step(args.variant, Xs.copy(order="F"), n, s)
+            warm += 1
         del Xs
     steps, work = [], None
     t_start = time.perf_counter()
@@ -277,7 +278,7 @@ def run_reference(args, rank, world):
     threads = os.cpu_count()
     sample = (f"{len(steps)} full-size {args.variant} QRs of m={m} x n={n}, s={s} by the numpy/OpenBLAS "
               f"restatement of the reference on {threads} host threads (steps bounded by a "
-              f"{args.ref_budget_s:.0f} s budget; warm-up: one QR of a 2^16-row sample)")
+              f"{args.ref_budget_s:.0f} s budget; each warm-up step: one QR of a 2^16-row sample)")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms",
         "n_gpus": args.gpus, "steps": len(steps), "steps_requested": args.steps, "warmup": warm,

@@ -57,7 +57,8 @@ def test_algorithmic_counts_at_config1():
 
 def test_reference_arm_runs_full_size_steps_within_budget():
     """--impl reference times whole QRs of the configured size (no scaling), runs
-    no more steps than asked or than the budget allows, and says how many ran."""
+    no more steps than asked or than the budget allows, says how many ran, and
+    runs the warm-up steps asked for."""
     import json
     import subprocess
     env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
@@ -67,7 +68,7 @@ def test_reference_arm_runs_full_size_steps_within_budget():
     assert r.returncode == 0, r.stderr[-2000:]
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["unit"] == "ms"
-    assert 1 <= line["steps"] <= 3 and line["steps_requested"] == 3 and line["warmup"] == 1
+    assert 1 <= line["steps"] <= 3 and line["steps_requested"] == 3 and line["warmup"] == 2
     assert len(line["step_ms"]) == line["steps"]
     assert abs(sum(line["step_ms"]) / line["steps"] - line["value"]) < 0.2
     assert "m=8192" in line["config"]["workload"]
