@@ -52,39 +52,77 @@ int tsqr_tile_rows(int nc) { return nc <= 32 ? 256 : BCGS_TSQR_TR64; }
 // Householder scalars.
 static size_t tsqr_tile_smem_bytes(int TR, int NC) { return (size_t)(TR * NC + NC) * sizeof(double); }
 
-// Sums of G values over the warp by an xor butterfly. Lane pairs add the same two
-// operands (a + b == b + a), so every lane ends with the same bits, in a fixed order.
-template <int G>
-__device__ __forceinline__ void warp_sum(double* w) {
+// Sum of one value over the warp by an xor butterfly. Lane pairs add the same two
+// operands (a + b == b + a), so every lane ends with the same bits.
+__device__ __forceinline__ double warp_sum1(double w) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    return w;
+}
+
+// One reflector H = I - t v v^T applied to column c: w = sum_r v[r] a[r][c] (lane
+// `lane` owns rows lane + 32 i, i < RPL), then a[r][c] -= w (t v[r]) with tv = t v.
+// v is zero above the reflector's pivot row, so those rows keep their values.
+template <int RPL>
+__device__ __forceinline__ void apply1(double* a, int TR, int c, const double* v, const double* tv, int lane) {
+    double w = 0.0;
 #pragma unroll
-        for (int g = 0; g < G; ++g) w[g] += __shfl_xor_sync(0xffffffffu, w[g], o);
+    for (int i = 0; i < RPL; ++i) w = fma(v[i], a[c * TR + lane + 32 * i], w);
+    w = warp_sum1(w);
+#pragma unroll
+    for (int i = 0; i < RPL; ++i) {
+        double* e = &a[c * TR + lane + 32 * i];
+        *e = fma(-w, tv[i], *e);
     }
 }
 
-// w_c = sum over the tile's rows of v[r] * a[r][c] for G columns c0.., then
-// a[r][c] -= (t w_c) v[r]. Lane `lane` owns rows lane + 32 i (i < RPL); v is zero
-// above the reflector's pivot row, so those rows are left as they are.
-template <int RPL, int G>
-__device__ __forceinline__ void apply_reflector(double* a, int TR, int c0, const double* v, double t, int lane) {
-    double w[G];
+// The same for the four columns c0 .. c0+3. The four sums are reduced together:
+// lane bit 4 splits the columns into pairs and bit 3 into singles (each lane adds
+// the partner's half it keeps), then bits 2-0 finish one column per group of 8
+// lanes by a butterfly; lanes 8g .. 8g+7 end with column g's sum, which is then
+// broadcast. Six FP64 additions per lane for four columns instead of twenty, in a
+// fixed order.
+template <int RPL>
+__device__ __forceinline__ void apply4(double* a, int TR, int c0, const double* v, const double* tv, int lane) {
+    double w[4];
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
+    for (int g = 0; g < 4; ++g) {
         w[g] = 0.0;
 #pragma unroll
         for (int i = 0; i < RPL; ++i) w[g] = fma(v[i], a[(c0 + g) * TR + lane + 32 * i], w[g]);
     }
-    warp_sum<G>(w);
+    const bool b4 = (lane & 16) != 0, b3 = (lane & 8) != 0;
+    double k0 = b4 ? w[2] : w[0], k1 = b4 ? w[3] : w[1];
+    const double s0 = b4 ? w[0] : w[2], s1 = b4 ? w[1] : w[3];
+    k0 += __shfl_xor_sync(0xffffffffu, s0, 16);
+    k1 += __shfl_xor_sync(0xffffffffu, s1, 16);
+    double k = b3 ? k1 : k0;
+    k += __shfl_xor_sync(0xffffffffu, b3 ? k0 : k1, 8);
+    k += __shfl_xor_sync(0xffffffffu, k, 4);
+    k += __shfl_xor_sync(0xffffffffu, k, 2);
+    k += __shfl_xor_sync(0xffffffffu, k, 1);
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-        const double tw = t * w[g];
+    for (int g = 0; g < 4; ++g) {
+        const double wg = __shfl_sync(0xffffffffu, k, 8 * g);
 #pragma unroll
         for (int i = 0; i < RPL; ++i) {
             double* e = &a[(c0 + g) * TR + lane + 32 * i];
-            *e = fma(-tw, v[i], *e);
+            *e = fma(-wg, tv[i], *e);
         }
     }
+}
+
+// Applies (v, tv) to the columns of group q (columns [4q, 4q + 4)) that lie in
+// [c_lo, nc): four at once when the whole group does.
+template <int RPL>
+__device__ __forceinline__ void apply_group(double* a, int TR, int q, int c_lo, int nc, const double* v,
+                                            const double* tv, int lane) {
+    const int g0 = 4 * q;
+    if (g0 >= c_lo && g0 + 4 <= nc) {
+        apply4<RPL>(a, TR, g0, v, tv, lane);
+        return;
+    }
+    for (int c = g0 > c_lo ? g0 : c_lo; c < g0 + 4 && c < nc; ++c) apply1<RPL>(a, TR, c, v, tv, lane);
 }
 
 template <int W>
@@ -92,36 +130,70 @@ __device__ __forceinline__ void tile_sync() {
     if (W == 1) __syncwarp(); else __syncthreads();
 }
 
-// Applies the reflector (v, t) to columns [c_begin, nc) of the tile: groups of 4
-// columns q = 0, 1, ... starting at c_begin go to warp q mod W, then the remaining
-// single columns continue the same count. Each column's sum is one warp's
-// butterfly, so the result does not depend on W. Group 0, which holds column
-// c_begin, always belongs to warp 0.
-template <int RPL, int W>
-__device__ __forceinline__ void apply_reflector_cols(double* a, int TR, int c_begin, int nc, const double* v,
-                                                     double t, int lane, int warp) {
-    const int ng = (nc - c_begin) / 4;
-    for (int q = warp; q < ng; q += W) apply_reflector<RPL, 4>(a, TR, c_begin + 4 * q, v, t, lane);
-    for (int c = c_begin + 4 * ng; c < nc; ++c)
-        if ((ng + (c - c_begin - 4 * ng)) % W == warp) apply_reflector<RPL, 1>(a, TR, c, v, t, lane);
+// Householder reflector of column c by the conventions of LAPACK's dlarfg
+// (beta = -sign(alpha) sqrt(alpha^2 + ||x||^2), tau = (beta - alpha)/beta,
+// v = x / (alpha - beta)), computed by one warp from the column in shared memory
+// and stored back in place: v below the diagonal, beta on it, tau in tau[c].
+template <int RPL>
+__device__ __forceinline__ void make_reflector(double* a, double* tau, int TR, int c, int lane) {
+    __syncwarp();   // the column's rows were just written by this warp's lanes
+    double x[RPL];
+    double p = 0.0;
+#pragma unroll
+    for (int i = 0; i < RPL; ++i) {
+        const int r = lane + 32 * i;
+        x[i] = a[c * TR + r];
+        if (r > c) p = fma(x[i], x[i], p);
+    }
+    p = warp_sum1(p);
+    const double alpha = a[c * TR + c];
+    double t = 0.0, beta = alpha, scal = 0.0;
+    if (p > 0.0) {
+        beta = -copysign(sqrt(alpha * alpha + p), alpha);
+        t = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < RPL; ++i) {
+        const int r = lane + 32 * i;
+        if (r > c) a[c * TR + r] = x[i] * scal;
+        else if (r == c) a[c * TR + r] = beta;
+    }
+    if (lane == 0) tau[c] = t;
+}
+
+// Reflector j (stored in column j) into registers: v (1 on the diagonal, zero
+// above) and tv = tau_j v.
+template <int RPL>
+__device__ __forceinline__ double load_reflector(const double* a, const double* tau, int TR, int j, int lane,
+                                                 double* v, double* tv) {
+    const double t = tau[j];
+#pragma unroll
+    for (int i = 0; i < RPL; ++i) {
+        const int r = lane + 32 * i;
+        v[i] = r > j ? a[j * TR + r] : (r == j ? 1.0 : 0.0);
+        tv[i] = t * v[i];
+    }
+    return t;
 }
 
 // W warps per tile, the tile in shared memory (lane L owns rows L, L+32, ...).
 // A: rows x nc (lda); tile `tile` covers rows [tile*TR, min(rows, (tile+1)*TR)).
-// Householder QR by the conventions of LAPACK's dgeqr2/dlarfg (column j:
-// beta = -sign(alpha) sqrt(alpha^2 + ||x||^2), tau = (beta - alpha)/beta,
-// v = x / (alpha - beta)), then the tile's R (upper, lower part zero) to Rst rows
-// [tile*nc, (tile+1)*nc) (ld ldr), then the explicit tile Q formed in place in
-// dorg2r's order (backward over the reflectors) and written to Q (ldq; may alias
-// A). Tiles shorter than nc rows are padded with zero rows; padded rows of Q are
-// not written. Every dot product is a warp butterfly sum, and every warp forms
-// the reflector from the same column with the same operations, so the result is
-// bit-identical run to run and for any W. smem holds tsqr_tile_smem_bytes(TR, NC).
+// Householder QR by the conventions of LAPACK's dgeqr2/dlarfg, then the tile's R
+// (upper, lower part zero) to Rst rows [tile*nc, (tile+1)*nc) (ld ldr), then the
+// explicit tile Q formed in place in dorg2r's order (backward over the reflectors)
+// and written to Q (ldq; may alias A). Tiles shorter than nc rows are padded with
+// zero rows; padded rows of Q are not written. smem holds
+// tsqr_tile_smem_bytes(TR, NC).
 //
-// One barrier per reflector: all warps read column j (the reflector), apply it to
-// their column groups, and meet; then warp 0 stores column j. The next step reads
-// and writes other columns, except in the backward phase, where column j is in
-// group 0 of step j - 1, which warp 0 itself applies.
+// The columns are dealt out in groups of four, group q to warp q mod W, and every
+// column is only ever updated by its group's warp. Each reflector is formed once,
+// by the warp owning its column, and published in shared memory: while applying
+// reflector j, the owner of column j+1 updates that column first and forms
+// reflector j+1 from it before its other columns (look-ahead), so one barrier per
+// reflector separates the steps. Every sum has a fixed order, so the result is
+// bit-identical run to run (for a given W).
 template <int NC, int W>
 __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, double* Q, i64 ldq,
                                double* __restrict__ Rst, i64 ldr, i64 tile, double* smem) {
@@ -131,6 +203,7 @@ __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, doubl
     double* tau = smem + TR * NC;
     const int lane = threadIdx.x & 31;
     const int warp = W == 1 ? 0 : (int)(threadIdx.x >> 5);
+    const int ngroups = (nc + 3) / 4;
     const i64 row0 = tile * TR;
     const i64 h = min((i64)TR, rows - row0);
     tile_sync<W>();
@@ -141,42 +214,26 @@ __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, doubl
             a[c * TR + r] = (r < h) ? A[row0 + r + (i64)c * lda] : 0.0;
         }
     tile_sync<W>();
-
-    for (int j = 0; j < nc; ++j) {
-        double v[RPL];
-        double p = 0.0;
-#pragma unroll
-        for (int i = 0; i < RPL; ++i) {
-            const int r = lane + 32 * i;
-            v[i] = a[j * TR + r];
-            if (r > j) p = fma(v[i], v[i], p);
-        }
-        warp_sum<1>(&p);
-        const double alpha = a[j * TR + j];
-        double t = 0.0, beta = alpha, scal = 0.0;
-        if (p > 0.0) {
-            beta = -copysign(sqrt(alpha * alpha + p), alpha);
-            t = (beta - alpha) / beta;
-            scal = 1.0 / (alpha - beta);
-        }
-#pragma unroll
-        for (int i = 0; i < RPL; ++i) {
-            const int r = lane + 32 * i;
-            v[i] = (r > j) ? v[i] * scal : (r == j ? 1.0 : 0.0);
-        }
-        if (t != 0.0) apply_reflector_cols<RPL, W>(a, TR, j + 1, nc, v, t, lane, warp);
-        tile_sync<W>();
-        if (warp == 0) {
-#pragma unroll
-            for (int i = 0; i < RPL; ++i) {
-                const int r = lane + 32 * i;
-                if (r > j) a[j * TR + r] = v[i];
-                else if (r == j) a[j * TR + r] = beta;
-            }
-            if (lane == 0) tau[j] = t;
-        }
-    }
+    if (warp == 0) make_reflector<RPL>(a, tau, TR, 0, lane);   // group 0 belongs to warp 0
     tile_sync<W>();
+
+    double v[RPL], tv[RPL];
+    for (int j = 0; j < nc; ++j) {
+        const double t = load_reflector<RPL>(a, tau, TR, j, lane, v, tv);
+        const int jn = j + 1;
+        if (jn < nc) {
+            const int qn = jn >> 2;                 // group of column j + 1
+            int q0 = qn + ((warp - qn) % W + W) % W; // this warp's first group at or after qn
+            if (q0 == qn) {
+                if (t != 0.0) apply_group<RPL>(a, TR, qn, jn, nc, v, tv, lane);
+                make_reflector<RPL>(a, tau, TR, jn, lane);
+                q0 += W;
+            }
+            if (t != 0.0)
+                for (int q = q0; q < ngroups; q += W) apply_group<RPL>(a, TR, q, jn, nc, v, tv, lane);
+        }
+        tile_sync<W>();
+    }
     // R to the stack (upper, lower zero).
     for (int e = threadIdx.x; e < nc * nc; e += 32 * W) {
         const int i = e % nc, c = e / nc;
@@ -184,24 +241,22 @@ __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, doubl
     }
     tile_sync<W>();
     // Explicit Q in place (dorg2r): for j = nc-1 .. 0, apply H_j to columns j+1..
-    // and set column j to (I - tau v v^T) e_j.
+    // and set column j to (I - tau v v^T) e_j (its owner, after the barrier that
+    // ends every warp's reading of reflector j).
     for (int j = nc - 1; j >= 0; --j) {
-        const double t = tau[j];
-        double v[RPL];
-#pragma unroll
-        for (int i = 0; i < RPL; ++i) {
-            const int r = lane + 32 * i;
-            v[i] = (r > j) ? a[j * TR + r] : (r == j ? 1.0 : 0.0);
+        const double t = load_reflector<RPL>(a, tau, TR, j, lane, v, tv);
+        if (t != 0.0 && j + 1 < nc) {
+            const int qn = (j + 1) >> 2;
+            for (int q = qn + ((warp - qn) % W + W) % W; q < ngroups; q += W)
+                apply_group<RPL>(a, TR, q, j + 1, nc, v, tv, lane);
         }
-        if (t != 0.0) apply_reflector_cols<RPL, W>(a, TR, j + 1, nc, v, t, lane, warp);
         tile_sync<W>();
-        if (warp == 0) {
+        if ((j >> 2) % W == warp) {
 #pragma unroll
             for (int i = 0; i < RPL; ++i) {
                 const int r = lane + 32 * i;
                 a[j * TR + r] = (r > j) ? -t * v[i] : (r == j ? 1.0 - t : 0.0);
             }
-            __syncwarp();
         }
     }
     tile_sync<W>();
