@@ -28,15 +28,16 @@ namespace bcgs {
 // divides the row count by TR / nc, so taller tiles mean fewer levels and fewer
 // flops, at the price of fewer tiles resident per SM. The reflector application
 // is split over W warps by groups of columns. Measured on GB300 at m = 2^23,
-// n = 512 (TSQR of block 1 per BCGSI+P-1S QR): nc = 64 with 256-row tiles and 8
-// warps (one tile per SM) 420 ms; 128-row tiles with 4 warps (three per SM) 632
-// ms, with 8 warps 709 ms; 256-row tiles with 16 warps 465 ms. nc = 32 with 4
-// warps 78.5 ms, 8 warps 91.5 ms. nc = 16 with one warp 17.8 ms, two 18.8 ms.
+// n = 512 (TSQR of block 1 per BCGSI+P-1S QR), 256-row tiles (one per SM at
+// nc = 64): nc = 64 with 4 warps 431 ms, 8 warps 353 ms, 16 warps 346 ms; nc = 32
+// with 2 warps 69.6 ms, 4 warps 64.2 ms, 8 warps 71.4 ms; nc = 16 with one warp
+// 16.4 ms. (With the earlier per-warp reflectors and per-column butterflies,
+// 128-row tiles were slower at every warp count: 632 ms with 4 warps at nc = 64.)
 #ifndef BCGS_TSQR_TR64
 #define BCGS_TSQR_TR64 256
 #endif
 #ifndef BCGS_TSQR_W64
-#define BCGS_TSQR_W64 8
+#define BCGS_TSQR_W64 16
 #endif
 #ifndef BCGS_TSQR_W32
 #define BCGS_TSQR_W32 4
