@@ -49,9 +49,10 @@ constexpr int tsqr_tile_warps() { return NC > 32 ? BCGS_TSQR_W64 : (NC > 16 ? BC
 
 int tsqr_tile_rows(int nc) { return nc <= 32 ? 256 : BCGS_TSQR_TR64; }
 
-// Shared memory of one tile: the TR x NC tile, column-major (ld TR), and its NC
-// Householder scalars.
-static size_t tsqr_tile_smem_bytes(int TR, int NC) { return (size_t)(TR * NC + NC) * sizeof(double); }
+// Shared memory of one tile: the TR x NC tile, column-major (ld TR), its NC
+// Householder scalars, and two TR-row slots for tau * v of the reflector being
+// applied and the next one.
+static size_t tsqr_tile_smem_bytes(int TR, int NC) { return (size_t)(TR * NC + NC + 2 * TR) * sizeof(double); }
 
 // Sum of one value over the warp by an xor butterfly. Lane pairs add the same two
 // operands (a + b == b + a), so every lane ends with the same bits.
@@ -136,7 +137,7 @@ __device__ __forceinline__ void tile_sync() {
 // v = x / (alpha - beta)), computed by one warp from the column in shared memory
 // and stored back in place: v below the diagonal, beta on it, tau in tau[c].
 template <int RPL>
-__device__ __forceinline__ void make_reflector(double* a, double* tau, int TR, int c, int lane) {
+__device__ __forceinline__ void make_reflector(double* a, double* tau, double* tvb, int TR, int c, int lane) {
     __syncwarp();   // the column's rows were just written by this warp's lanes
     double x[RPL];
     double p = 0.0;
@@ -155,26 +156,43 @@ __device__ __forceinline__ void make_reflector(double* a, double* tau, int TR, i
         scal = 1.0 / (alpha - beta);
     }
     __syncwarp();
+    double* tv = tvb + (c & 1) * TR;
 #pragma unroll
     for (int i = 0; i < RPL; ++i) {
         const int r = lane + 32 * i;
-        if (r > c) a[c * TR + r] = x[i] * scal;
+        const double vr = x[i] * scal;
+        if (r > c) a[c * TR + r] = vr;
         else if (r == c) a[c * TR + r] = beta;
+        tv[r] = r > c ? t * vr : (r == c ? t : 0.0);
     }
     if (lane == 0) tau[c] = t;
 }
 
-// Reflector j (stored in column j) into registers: v (1 on the diagonal, zero
-// above) and tv = tau_j v.
+// tau_c * v_c of the reflector stored in column c, into slot c & 1 (one warp).
 template <int RPL>
-__device__ __forceinline__ double load_reflector(const double* a, const double* tau, int TR, int j, int lane,
-                                                 double* v, double* tv) {
+__device__ __forceinline__ void publish_tv(const double* a, const double* tau, double* tvb, int TR, int c,
+                                           int lane) {
+    const double t = tau[c];
+    double* tv = tvb + (c & 1) * TR;
+#pragma unroll
+    for (int i = 0; i < RPL; ++i) {
+        const int r = lane + 32 * i;
+        tv[r] = r > c ? t * a[c * TR + r] : (r == c ? t : 0.0);
+    }
+}
+
+// Reflector j (stored in column j) into registers: v (1 on the diagonal, zero
+// above) and tv = tau_j v from its published slot.
+template <int RPL>
+__device__ __forceinline__ double load_reflector(const double* a, const double* tau, const double* tvb, int TR,
+                                                 int j, int lane, double* v, double* tv) {
     const double t = tau[j];
+    const double* tj = tvb + (j & 1) * TR;
 #pragma unroll
     for (int i = 0; i < RPL; ++i) {
         const int r = lane + 32 * i;
         v[i] = r > j ? a[j * TR + r] : (r == j ? 1.0 : 0.0);
-        tv[i] = t * v[i];
+        tv[i] = tj[r];
     }
     return t;
 }
@@ -202,6 +220,7 @@ __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, doubl
     constexpr int RPL = TR / 32;
     double* a = smem;              // a[c * TR + r]
     double* tau = smem + TR * NC;
+    double* tvb = tau + NC;        // tau * v of reflectors j and j + 1 (slots j & 1)
     const int lane = threadIdx.x & 31;
     const int warp = W == 1 ? 0 : (int)(threadIdx.x >> 5);
     const int ngroups = (nc + 3) / 4;
@@ -215,19 +234,19 @@ __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, doubl
             a[c * TR + r] = (r < h) ? A[row0 + r + (i64)c * lda] : 0.0;
         }
     tile_sync<W>();
-    if (warp == 0) make_reflector<RPL>(a, tau, TR, 0, lane);   // group 0 belongs to warp 0
+    if (warp == 0) make_reflector<RPL>(a, tau, tvb, TR, 0, lane);   // group 0 belongs to warp 0
     tile_sync<W>();
 
     double v[RPL], tv[RPL];
     for (int j = 0; j < nc; ++j) {
-        const double t = load_reflector<RPL>(a, tau, TR, j, lane, v, tv);
+        const double t = load_reflector<RPL>(a, tau, tvb, TR, j, lane, v, tv);
         const int jn = j + 1;
         if (jn < nc) {
             const int qn = jn >> 2;                 // group of column j + 1
             int q0 = qn + ((warp - qn) % W + W) % W; // this warp's first group at or after qn
             if (q0 == qn) {
                 if (t != 0.0) apply_group<RPL>(a, TR, qn, jn, nc, v, tv, lane);
-                make_reflector<RPL>(a, tau, TR, jn, lane);
+                make_reflector<RPL>(a, tau, tvb, TR, jn, lane);
                 q0 += W;
             }
             if (t != 0.0)
@@ -243,9 +262,13 @@ __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, doubl
     tile_sync<W>();
     // Explicit Q in place (dorg2r): for j = nc-1 .. 0, apply H_j to columns j+1..
     // and set column j to (I - tau v v^T) e_j (its owner, after the barrier that
-    // ends every warp's reading of reflector j).
+    // ends every warp's reading of reflector j). tau * v of reflector j - 1 is
+    // published during step j by the owner of column j - 1.
+    if (((nc - 1) >> 2) % W == warp) publish_tv<RPL>(a, tau, tvb, TR, nc - 1, lane);
+    tile_sync<W>();
     for (int j = nc - 1; j >= 0; --j) {
-        const double t = load_reflector<RPL>(a, tau, TR, j, lane, v, tv);
+        const double t = load_reflector<RPL>(a, tau, tvb, TR, j, lane, v, tv);
+        if (j >= 1 && ((j - 1) >> 2) % W == warp) publish_tv<RPL>(a, tau, tvb, TR, j - 1, lane);
         if (t != 0.0 && j + 1 < nc) {
             const int qn = (j + 1) >> 2;
             for (int q = qn + ((warp - qn) % W + W) % W; q < ngroups; q += W)
@@ -256,7 +279,7 @@ __device__ void tsqr_tile_body(const double* A, i64 lda, i64 rows, int nc, doubl
 #pragma unroll
             for (int i = 0; i < RPL; ++i) {
                 const int r = lane + 32 * i;
-                a[j * TR + r] = (r > j) ? -t * v[i] : (r == j ? 1.0 - t : 0.0);
+                a[j * TR + r] = (r > j) ? -tv[i] : (r == j ? 1.0 - t : 0.0);
             }
         }
     }
