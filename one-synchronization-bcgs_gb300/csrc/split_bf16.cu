@@ -180,8 +180,9 @@ __global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c
 // column loads and the digits, staged in shared memory as [plane][64-row
 // half][column][64 rows]. That is the store's own layout: for one plane and one
 // 64-row chunk, the 16 columns' runs of 64 rows are one contiguous 2 KB block of
-// HBM. A full tile leaves as 2 KD bulk copies of 2 KB, issued by as many threads.
-// Ragged tiles (rows past m, or fewer than 16 columns) are stored element-wise.
+// HBM. A tile of 128 whole rows leaves as 2 KD bulk copies (128 bytes per valid
+// column), issued by as many threads; a tile with rows past m is stored
+// element-wise.
 template <int KD>
 __device__ __forceinline__ void slice_body(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
                                            const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
@@ -203,7 +204,12 @@ __device__ __forceinline__ void slice_body(const double* __restrict__ X, i64 ld,
 #pragma unroll
         for (int i = 0; i < KD; ++i) sdig[i][t >> 6][j][t & 63] = bf16_bits_of_int(d[i]);
     }
-    const bool full = (r0 + 128 <= m) && (g + CG <= nc);
+    // A tile whose 128 rows all lie below m leaves as bulk copies of its valid
+    // columns (ncols x 128 bytes per plane and 64-row half: the store keeps a
+    // plane's columns of one chunk contiguous, so a group narrower than 16 columns,
+    // as blocks of s = 4 or 8 give, is still one contiguous block).
+    const int ncols = nc - g < CG ? nc - g : CG;
+    const bool full = r0 + 128 <= m;
     if (full) tc::fence_proxy_async_smem();
     __syncthreads();
     // Element (r, c) of plane i at ((i*nrc + r/64)*n + c)*64 + r%64.
@@ -211,7 +217,7 @@ __device__ __forceinline__ void slice_body(const double* __restrict__ X, i64 ld,
         if (t < 2 * KD) {
             const int i = t >> 1, h = t & 1;
             unsigned short* dst = colstore + (((i64)i * nrc + r0 / 64 + h) * n + (c0 + g)) * 64;
-            tc::bulk_store(dst, &sdig[i][h][0][0], CG * 64 * 2);
+            tc::bulk_store(dst, &sdig[i][h][0][0], ncols * 64 * 2);
             tc::bulk_commit();
             tc::bulk_wait_read();
         }
