@@ -67,7 +67,7 @@ def parse():
     ap.add_argument("--e2e-cuda-host-alloc", action="store_true",
                     help="add an e2e leg on cudaHostAlloc host buffers beside the huge-page ones")
     ap.add_argument("--e2e-pageable", action="store_true",
-                    help="add an e2e leg on pageable (malloc) host buffers, one sample")
+                    help="add an e2e leg on pageable (malloc) host buffers, two samples")
     ap.add_argument("--cpu-rows", type=int, default=1 << 21,
                     help="rows of the bounded CPU sample of the cpu_baseline leg (time scaled to m)")
     ap.add_argument("--ref-budget-s", type=float, default=180.0,
@@ -432,12 +432,24 @@ def run_ours(args, rank, world, local_rank):
                                       "path": "the same call on cudaHostAlloc buffers (torch pin_memory)"}
             del Xc, Rc
         if args.e2e_pageable:
-            Xq = np.zeros((m, n), order="F")
-            Rq = np.zeros((n, n), order="F")
-            t3, tl3 = host_leg(Xq, Rq, 1)
+            # Pageable memory from the C library's malloc, as the reference's own
+            # driver allocates Xsub (numpy would advise huge pages on its arrays).
+            import ctypes
+            libc = ctypes.CDLL(None)
+            libc.malloc.restype = ctypes.c_void_p
+            libc.malloc.argtypes = [ctypes.c_size_t]
+            libc.free.argtypes = [ctypes.c_void_p]
+            px, pr = libc.malloc(m * n * 8), libc.malloc(n * n * 8)
+            if not px or not pr:
+                raise RuntimeError("malloc failed")
+            Xq = np.ctypeslib.as_array((ctypes.c_double * (m * n)).from_address(px)).reshape((m, n), order="F")
+            Rq = np.ctypeslib.as_array((ctypes.c_double * (n * n)).from_address(pr)).reshape((n, n), order="F")
+            t3, tl3 = host_leg(Xq, Rq, 2)
             e2e["pageable"] = {"value": round(sum(t3) / len(t3), 3), "samples_ms": [round(x, 1) for x in t3],
-                               "timeline_ms": tl3, "path": "the same call on ordinary (pageable) numpy buffers"}
+                               "timeline_ms": tl3, "path": "the same call on malloc'd (pageable) buffers"}
             del Xq, Rq
+            libc.free(px)
+            libc.free(pr)
 
     # FP64 leg and 48-bit split leg beside the 56-bit split run.
     fp64_ms = fp64_acc = fast_ms = fast_acc = None

@@ -10,6 +10,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <climits>
+#include <deque>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -21,6 +22,7 @@
 #include "../../include/orth_gb300.h"
 #include "common.cuh"
 #include "kernels.h"
+#include "host_stage.h"
 #include "split.h"
 
 namespace bcgs {
@@ -277,6 +279,12 @@ struct HostLink {
     std::atomic<int> err{0};
     int dev = 0;
 
+    // Page-locked staging slots for a pageable X (null: the driver's own path).
+    HostStage* stage = nullptr;
+    std::vector<cudaEvent_t> up_ev, dn_ev;   // slot i's last copy engine transfer
+    std::vector<char> up_used;
+    int up_next = 0;
+
     // Worker threads (pageable path).
     struct Req { cudaEvent_t ev; int c0, c1; };
     std::thread up, down;
@@ -298,13 +306,81 @@ struct HostLink {
         int z = 0;
         err.compare_exchange_strong(z, e);
     }
-    // Issue chunk k of X and record its event (either thread).
+    // Contiguous pieces of columns [c0, c0 + nc) of X, at most one slot each:
+    // f(host pointer, device pointer, bytes) in column order.
+    template <class F>
+    int for_pieces(int c0, int nc, size_t max_bytes, F f) {
+        const size_t col = (size_t)m * sizeof(double);
+        auto split = [&](char* h, char* d, size_t bytes) -> int {
+            for (size_t off = 0; off < bytes; off += max_bytes) {
+                const int e = f(h + off, d + off, std::min(max_bytes, bytes - off));
+                if (e) return e;
+            }
+            return 0;
+        };
+        if (ldh == m)
+            return split(reinterpret_cast<char*>(hX + (i64)c0 * m), reinterpret_cast<char*>(dX + (i64)c0 * m),
+                         col * (size_t)nc);
+        for (int c = c0; c < c0 + nc; ++c) {
+            const int e = split(reinterpret_cast<char*>(hX + (i64)c * ldh), reinterpret_cast<char*>(dX + (i64)c * m),
+                                col);
+            if (e) return e;
+        }
+        return 0;
+    }
+    // Issue chunk k of X and record its event (either thread). Through the
+    // staging slots: host threads copy a piece into a free slot while the copy
+    // engine moves the previous ones.
     int put_chunk(int k) {
         const int c0 = k * chunk;
         const int nc = n - c0 < chunk ? n - c0 : chunk;
-        int e = (int)copy(dX, m, hX, ldh, c0, nc, cudaMemcpyHostToDevice, cin);
+        int e = 0;
+        if (stage) {
+            e = for_pieces(c0, nc, stage->slot_bytes, [&](char* h, char* d, size_t bytes) -> int {
+                const int sl = up_next++ % (int)stage->up.size();
+                if (up_used[sl]) {
+                    const int ee = (int)cudaEventSynchronize(up_ev[sl]);
+                    if (ee) return ee;
+                }
+                stage->pool->copy(stage->up[sl], h, bytes);
+                int ee = (int)cudaMemcpyAsync(d, stage->up[sl], bytes, cudaMemcpyHostToDevice, cin);
+                if (!ee) ee = (int)cudaEventRecord(up_ev[sl], cin);
+                up_used[sl] = 1;
+                return ee;
+            });
+        } else {
+            e = (int)copy(dX, m, hX, ldh, c0, nc, cudaMemcpyHostToDevice, cin);
+        }
         if (!e) e = (int)cudaEventRecord(ev_in[k], cin);
         return e;
+    }
+    // Q columns [c0, c1) to the host through the download slots, after event ev on
+    // the compute stream. In flight: (slot, host destination, bytes) whose copy
+    // engine transfer is issued; the host copy out of a slot waits for it.
+    struct Pending { int slot; char* h; size_t bytes; };
+    std::deque<Pending> dn_fifo;
+    int dn_next = 0;
+    int drain_one() {
+        const Pending q = dn_fifo.front();
+        dn_fifo.pop_front();
+        const int e = (int)cudaEventSynchronize(dn_ev[q.slot]);
+        if (!e && !err) stage->pool->copy(q.h, stage->down[q.slot], q.bytes);
+        return e;
+    }
+    int get_cols_staged(const Req& r) {
+        int e = (int)cudaStreamWaitEvent(cout, r.ev, 0);
+        if (e) return e;
+        return for_pieces(r.c0, r.c1 - r.c0, stage->slot_bytes, [&](char* h, char* d, size_t bytes) -> int {
+            const int sl = dn_next++ % (int)stage->down.size();
+            if ((int)dn_fifo.size() == (int)stage->down.size()) {   // the oldest holds this slot
+                const int ee = drain_one();
+                if (ee) return ee;
+            }
+            int ee = (int)cudaMemcpyAsync(stage->down[sl], d, bytes, cudaMemcpyDeviceToHost, cout);
+            if (!ee) ee = (int)cudaEventRecord(dn_ev[sl], cout);
+            if (!ee) dn_fifo.push_back(Pending{sl, h, bytes});
+            return ee;
+        });
     }
     // Enqueue every H2D chunk on cin (after `st` reaches this point).
     void start(cudaStream_t st) {
@@ -322,6 +398,15 @@ struct HostLink {
             cudaEvent_t ek = nullptr;
             if ((e = (int)cudaEventCreateWithFlags(&ek, cudaEventDisableTiming))) { fail(e); return; }
             ev_in.push_back(ek);
+        }
+        if (pageable) stage = host_stage();
+        if (stage) {
+            for (size_t i = 0; i < stage->up.size() + stage->down.size(); ++i) {
+                cudaEvent_t ek = nullptr;
+                if ((e = (int)cudaEventCreateWithFlags(&ek, cudaEventDisableTiming))) { fail(e); return; }
+                (i < stage->up.size() ? up_ev : dn_ev).push_back(ek);
+            }
+            up_used.assign(stage->up.size(), 0);
         }
         if (!pageable) {
             for (int k = 0; k < nchunks && !err; ++k)
@@ -390,14 +475,32 @@ struct HostLink {
                     Req r;
                     {
                         std::unique_lock<std::mutex> lock(mu);
+                        if (reqs.empty() && !closing && stage && !dn_fifo.empty()) {
+                            // Nothing new to issue: move landed columns out meanwhile.
+                            lock.unlock();
+                            const int e2 = drain_one();
+                            if (e2) fail(e2);
+                            continue;
+                        }
                         cv.wait(lock, [&] { return !reqs.empty() || closing; });
-                        if (reqs.empty()) return;
+                        if (reqs.empty()) {   // closing: the last columns out of the slots
+                            lock.unlock();
+                            while (stage && !dn_fifo.empty()) {
+                                const int e2 = drain_one();
+                                if (e2) fail(e2);
+                            }
+                            return;
+                        }
                         r = reqs.front();
                         reqs.erase(reqs.begin());
                     }
                     if (err) continue;   // drain the queue without copying
-                    e = (int)cudaStreamWaitEvent(cout, r.ev, 0);
-                    if (!e) e = (int)copy(hX, ldh, dX, m, r.c0, r.c1 - r.c0, cudaMemcpyDeviceToHost, cout);
+                    if (stage) {
+                        e = get_cols_staged(r);
+                    } else {
+                        e = (int)cudaStreamWaitEvent(cout, r.ev, 0);
+                        if (!e) e = (int)copy(hX, ldh, dX, m, r.c0, r.c1 - r.c0, cudaMemcpyDeviceToHost, cout);
+                    }
                     if (e) fail(e);
                 }
             });
@@ -436,6 +539,10 @@ struct HostLink {
         ev_in.clear();
         for (cudaEvent_t e : ev_out) cudaEventDestroy(e);
         ev_out.clear();
+        for (cudaEvent_t e : up_ev) cudaEventDestroy(e);
+        up_ev.clear();
+        for (cudaEvent_t e : dn_ev) cudaEventDestroy(e);
+        dn_ev.clear();
         if (ev_fin) cudaEventDestroy(ev_fin);
         ev_fin = nullptr;
     }
@@ -1583,6 +1690,7 @@ void orth_gb300_release(void) {
     if (g_ctx.hostR_stage) cudaFreeHost(g_ctx.hostR_stage);
     g_ctx.hostR_stage = nullptr;
     g_ctx.hostR_stage_bytes = 0;
+    host_stage_release();
 }
 
 const char* orth_gb300_version(void) { return "orth_gb300 0.1 (sm_103a)"; }
