@@ -1591,7 +1591,8 @@ __global__ void spread_error(const int* __restrict__ err, int* __restrict__ dsta
 constexpr size_t kBbuildSmem = 3 * 64 * 65 * sizeof(double);
 
 enum SKind {
-    kSZero, kSColmax, kSSlice, kSGram, kSReduce, kSSmall, kSBbuild, kSBdigit, kSUpdate, kSTile, kSRoot, kSApply,
+    kSZero, kSColmax, kSSlice, kSGram, kSReduce, kSSmall, kSBbuild, kSBdigit, kSUpdate, kSUpdate16, kSTile, kSRoot,
+    kSApply,
     kSZeroBuf
 };
 struct SLaunch {
@@ -1707,6 +1708,7 @@ int plan_wave(SplitStaged& S, SWave& W) {
             for (int q = 0; q < 3 && !rc; ++q)
                 rc = make_map3(&P.map_col_u_part[q], P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 16 * (q + 1),
                                2);
+            if (!rc) rc = make_map3(&P.map_bdig16, P.bdig, P.kpad, 16, KD_MAX, P.kpad, 16 * P.kpad, 16);
             if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
             if (rc) return rc;
         }
@@ -1843,12 +1845,15 @@ int plan_wave(SplitStaged& S, SWave& W) {
     std::vector<int> bc;
     std::vector<BdigitJob> dj;
     std::vector<int> dc;
-    std::vector<SplitUpdJob> uj;
-    std::vector<int> ut;
-    // finish_update for one matrix: kin digit columns in, nout (<= 32) columns out at c0.
+    std::vector<SplitUpdJob> uj, uj16;
+    std::vector<int> ut, ut16;
+    // finish_update for one matrix: kin digit columns in, nout (<= 32) columns out at
+    // c0; as finish_update, 16-column tiles when nout <= 16 (blocks of s <= 8), each
+    // width one batched launch.
     auto finish = [&](SMat& M, int kin, int c0, int nout) {
         Plan& P = M.P;
-        dj.push_back({P.bfull, (int)P.kpad, kin - nout, nout, 32, (int)P.kpad, P.bmax, P.fexp, P.bdig});
+        const int NB = nout <= 16 ? 16 : 32;
+        dj.push_back({P.bfull, (int)P.kpad, kin - nout, nout, NB, (int)P.kpad, P.bmax, P.fexp, P.bdig});
         dc.push_back((int)ceil_div(P.kpad, 256));
         uz.push_back({P.cmax + c0, (int)(nout * sizeof(unsigned long long))});
         UpdateParams up{};
@@ -1860,10 +1865,10 @@ int plan_wave(SplitStaged& S, SWave& W) {
         std::memset(&J, 0, sizeof(J));
         J.mapA = P.map_col_u;
         J.mapAlast = up.kr_last < KCH ? P.map_col_u_part[up.kr_last / 16 - 1] : P.map_col_u;
-        J.mapB = P.map_bdig32;
+        J.mapB = NB == 16 ? P.map_bdig16 : P.map_bdig32;
         J.p = up;
-        uj.push_back(J);
-        ut.push_back((int)ceil_div(P.m, TILE_M));
+        (NB == 16 ? uj16 : uj).push_back(J);
+        (NB == 16 ? ut16 : ut).push_back((int)ceil_div(P.m, TILE_M));
         for (int c = c0; c < c0 + nout; ++c) { P.fresh[c] = 0; P.cmax_valid[c] = 1; }
     };
     // Engine::update (launch_update_split): X[:, c0:c0+nc] = (X_c - X[:, 0:K] S) T^{-1}, c0 == K.
@@ -1894,13 +1899,14 @@ int plan_wave(SplitStaged& S, SWave& W) {
     };
     auto flush_update = [&]() {
         flush_prepare();
-        if (uj.empty()) return;
-        if (S.device) uz.push_back({S.dtile, (int)sizeof(int)});
+        if (uj.empty() && uj16.empty()) return;
+        if (S.device) uz.push_back({S.dtile, (int)(2 * sizeof(int))});   // both launches' tile counters
         push_zero(uz);
         push(kSBbuild, bj, bc);
         push(kSBdigit, dj, dc);
-        push(kSUpdate, uj, ut);
-        uz.clear(); bj.clear(); bc.clear(); dj.clear(); dc.clear(); uj.clear(); ut.clear();
+        if (!uj.empty()) push(kSUpdate, uj, ut);
+        if (!uj16.empty()) push(kSUpdate16, uj16, ut16);
+        uz.clear(); bj.clear(); bc.clear(); dj.clear(); dc.clear(); uj.clear(); ut.clear(); uj16.clear(); ut16.clear();
     };
 
     // ---- TSQR of block 1 (the single-panel tree of launch_tsqr, per matrix) ----
@@ -2180,6 +2186,20 @@ int enqueue_wave(SplitStaged& S, SWave& W, cudaStream_t st) {
                 ++g_launch_count;
                 break;
             }
+            case kSUpdate16: {   // its own tile counter: the word after the 32-column launch's
+                const auto* J = reinterpret_cast<const SplitUpdJob*>(jb + L.job_off);
+                const unsigned grid = items < (unsigned)S.num_sms ? items : (unsigned)S.num_sms;
+                UpdateParams u16 = u0;
+                u16.tile_ctr = S.dtile + 1;
+                if (KD == 6)
+                    update_tc_kernel<16, 6, true><<<grid, UTHREADS, SmemLayout<16, 6>::BYTES, st>>>(none, none, none, u16,
+                                                                                                   J, pre, L.njobs);
+                else
+                    update_tc_kernel<16, 7, true><<<grid, UTHREADS, SmemLayout<16, 7>::BYTES, st>>>(none, none, none, u16,
+                                                                                                   J, pre, L.njobs);
+                ++g_launch_count;
+                break;
+            }
             case kSTile:
                 rc = launch_tsqr_tile_batched(reinterpret_cast<const TsqrTileJob*>(jb + L.job_off), pre, L.njobs,
                                               L.items, 16, st);
@@ -2281,6 +2301,8 @@ int split_staged_create(int count, const int* m, const int* n, const int* s, dou
     if (!rc) rc = set_smem(gram_tc_kernel<7, 6, true>, SmemLayout<32, 7>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<32, 6, true>, SmemLayout<32, 6>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<32, 7, true>, SmemLayout<32, 7>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<16, 6, true>, SmemLayout<16, 6>::BYTES);
+    if (!rc) rc = set_smem(update_tc_kernel<16, 7, true>, SmemLayout<16, 7>::BYTES);
     if (!rc) rc = set_smem(bbuild_batched, (int)kBbuildSmem);
     if (!rc) rc = tsqr_tile_batched_prepare();
     if (rc) { free_staged(S); return 3; }
