@@ -712,12 +712,11 @@ struct SplitGramJob {   // the CUtensorMap members keep the struct 64-byte align
 // BATCH: the CTAs of many Grams in one launch; CTA b runs item b - prefix[j] of
 // job j (prefix[j] <= b < prefix[j + 1]) with job j's maps and parameters, and
 // exactly the arithmetic of a single launch of that Gram. p0.err is the launch's.
-template <int KD, int KA, bool BATCH>
+template <int NB, int KD, int KA, bool BATCH>
 __global__ void __launch_bounds__(NTHREADS, 1)
 gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapAlast,
                const __grid_constant__ CUtensorMap mapB, GramParams p0, const SplitGramJob* __restrict__ jobs,
                const int* __restrict__ prefix, int njobs) {
-    constexpr int NB = 32;
     using L = SmemLayout<NB, KD>;
     extern __shared__ uint8_t smem_raw[];
     __shared__ uint32_t tmem_slot;
@@ -1167,7 +1166,7 @@ struct Plan {
     double *bfull = nullptr, *part = nullptr;
     i64 part_doubles = 0;
     // maps
-    CUtensorMap map_col_a, map_col_b, map_col_u, map_bdig16, map_bdig32;
+    CUtensorMap map_col_a, map_col_b, map_col_b16, map_col_u, map_bdig16, map_bdig32;
     CUtensorMap map_col_a_part[7];   // Gram A boxes of 16, 32, ..., 112 columns (a partial last M-block)
     CUtensorMap map_col_u_part[3];   // update A boxes of 16, 32, 48 columns x two 64-row chunks
     int kd = 7;
@@ -1303,6 +1302,7 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     // Chunked stores as 3-D tensors {64, columns or rows, plane x chunk}.
     int rc = make_map3(&P.map_col_a, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, TILE_M);
     if (!rc) rc = make_map3(&P.map_col_b, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 32);
+    if (!rc) rc = make_map3(&P.map_col_b16, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 16);
     // Update A tiles: 64 columns of two adjacent 64-row chunks (128 rows).
     if (!rc) rc = make_map3(&P.map_col_u, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, KCH, 2);
     // Partial boxes: a Gram's last M-block of fewer than 128 columns, an update's
@@ -1315,9 +1315,12 @@ int split_begin(double* X, i64 ld, i64 m, int n, int s, int kd, char* ws, size_t
     if (!rc) rc = make_map3(&P.map_bdig32, P.bdig, P.kpad, 32, KD_MAX, P.kpad, 32 * P.kpad, 32);
     if (rc) return rc;
     // Shared-memory limits of the tensor-core kernels on this device.
-    rc = set_smem(gram_tc_kernel<6, 6, false>, SmemLayout<32, 6>::BYTES);
-    if (!rc) rc = set_smem(gram_tc_kernel<7, 7, false>, SmemLayout<32, 7>::BYTES);
-    if (!rc) rc = set_smem(gram_tc_kernel<7, 6, false>, SmemLayout<32, 7>::BYTES);
+    rc = set_smem(gram_tc_kernel<32, 6, 6, false>, SmemLayout<32, 6>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<32, 7, 7, false>, SmemLayout<32, 7>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<32, 7, 6, false>, SmemLayout<32, 7>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<16, 6, 6, false>, SmemLayout<16, 6>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<16, 7, 7, false>, SmemLayout<16, 7>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<16, 7, 6, false>, SmemLayout<16, 7>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<16, 6, false>, SmemLayout<16, 6>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<16, 7, false>, SmemLayout<16, 7>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<32, 6, false>, SmemLayout<32, 6>::BYTES);
@@ -1370,8 +1373,9 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     if (rc) return rc;
     GramParams gp;
     gp.na = na; gp.nb = nb; gp.b0 = b0; gp.m = m;
+    const int NB = nb <= 16 ? 16 : 32;   // a 16-column N group for narrow B (blocks of s <= 8)
     gp.numMB = (int)ceil_div(na, TILE_M);
-    gp.numNG = (int)ceil_div(nb, 32);
+    gp.numNG = (int)ceil_div(nb, NB);
     const int mbn = gp.numMB * gp.numNG;
     gp.rc = num_sms / mbn > 0 ? num_sms / mbn : 1;
     gp.rows_per = round_up(ceil_div(m, gp.rc), (i64)ROW_ALIGN);
@@ -1388,16 +1392,17 @@ int launch_gram_split(const double* X, i64 ld, i64 m, int na, int b0, int nb, do
     gp.alast = (int)round_up(na - (i64)(gp.numMB - 1) * TILE_M, 16);
     const CUtensorMap& alast_map = gp.alast < TILE_M ? P.map_col_a_part[gp.alast / 16 - 1] : P.map_col_a;
     const unsigned grid = (unsigned)(mbn * gp.rc);
-    const int smem = P.kd == 6 ? SmemLayout<32, 6>::BYTES : SmemLayout<32, 7>::BYTES;
-    if (P.kd == 6)
-        gram_tc_kernel<6, 6, false><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp, nullptr,
-                                                                  nullptr, 0);
-    else if (gram_a_planes(P.kd) == 6)
-        gram_tc_kernel<7, 6, false><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp, nullptr,
-                                                                  nullptr, 0);
-    else
-        gram_tc_kernel<7, 7, false><<<grid, NTHREADS, smem, st>>>(P.map_col_a, alast_map, P.map_col_b, gp, nullptr,
-                                                                  nullptr, 0);
+    const CUtensorMap& bmap = NB == 16 ? P.map_col_b16 : P.map_col_b;
+    const int ka = gram_a_planes(P.kd);
+#define BCGS_GRAM(NBT, KDT, KAT)                                                                                  \
+    gram_tc_kernel<NBT, KDT, KAT, false><<<grid, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(                \
+        P.map_col_a, alast_map, bmap, gp, nullptr, nullptr, 0)
+    if (NB == 16) {
+        if (P.kd == 6) BCGS_GRAM(16, 6, 6); else if (ka == 6) BCGS_GRAM(16, 7, 6); else BCGS_GRAM(16, 7, 7);
+    } else {
+        if (P.kd == 6) BCGS_GRAM(32, 6, 6); else if (ka == 6) BCGS_GRAM(32, 7, 6); else BCGS_GRAM(32, 7, 7);
+    }
+#undef BCGS_GRAM
     g_launch_count += 1;
     rc = (int)cudaGetLastError();
     if (rc) return rc;
@@ -1591,7 +1596,7 @@ __global__ void spread_error(const int* __restrict__ err, int* __restrict__ dsta
 constexpr size_t kBbuildSmem = 3 * 64 * 65 * sizeof(double);
 
 enum SKind {
-    kSZero, kSColmax, kSSlice, kSGram, kSReduce, kSSmall, kSBbuild, kSBdigit, kSUpdate, kSUpdate16, kSTile, kSRoot,
+    kSZero, kSColmax, kSSlice, kSGram, kSGram16, kSReduce, kSSmall, kSBbuild, kSBdigit, kSUpdate, kSUpdate16, kSTile, kSRoot,
     kSApply,
     kSZeroBuf
 };
@@ -1702,6 +1707,7 @@ int plan_wave(SplitStaged& S, SWave& W) {
             const int n = M.n;
             int rc = make_map3(&P.map_col_a, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, TILE_M);
             if (!rc) rc = make_map3(&P.map_col_b, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 32);
+            if (!rc) rc = make_map3(&P.map_col_b16, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 16);
             if (!rc) rc = make_map3(&P.map_col_u, P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, KCH, 2);
             for (int q = 0; q < 7 && !rc; ++q)
                 rc = make_map3(&P.map_col_a_part[q], P.colstore, 64, n, KD_MAX * P.nrc, 64, (i64)n * 64, 16 * (q + 1));
@@ -1768,8 +1774,8 @@ int plan_wave(SplitStaged& S, SWave& W) {
         }
     };
 
-    std::vector<SplitGramJob> gj;
-    std::vector<int> gc;
+    std::vector<SplitGramJob> gj, gj16;
+    std::vector<int> gc, gc16;
     std::vector<GramJob> rj;
     std::vector<int> rc2;
     bool too_big = false;   // a Gram's partials would not fit the matrix's buffer
@@ -1779,8 +1785,9 @@ int plan_wave(SplitStaged& S, SWave& W) {
         Plan& P = M.P;
         GramParams gp{};
         gp.na = na; gp.nb = nb; gp.b0 = b0; gp.m = P.m;
+        const int NB = nb <= 16 ? 16 : 32;   // as launch_gram_split
         gp.numMB = (int)ceil_div(na, TILE_M);
-        gp.numNG = (int)ceil_div(nb, 32);
+        gp.numNG = (int)ceil_div(nb, NB);
         const int mbn = gp.numMB * gp.numNG;
         gp.rc = S.num_sms / mbn > 0 ? S.num_sms / mbn : 1;
         gp.rows_per = round_up(ceil_div(P.m, gp.rc), (i64)ROW_ALIGN);
@@ -1796,10 +1803,10 @@ int plan_wave(SplitStaged& S, SWave& W) {
         std::memset(&J, 0, sizeof(J));
         J.mapA = P.map_col_a;
         J.mapAlast = gp.alast < TILE_M ? P.map_col_a_part[gp.alast / 16 - 1] : P.map_col_a;
-        J.mapB = P.map_col_b;
+        J.mapB = NB == 16 ? P.map_col_b16 : P.map_col_b;
         J.p = gp;
-        gj.push_back(J);
-        gc.push_back(mbn * gp.rc);
+        (NB == 16 ? gj16 : gj).push_back(J);
+        (NB == 16 ? gc16 : gc).push_back(mbn * gp.rc);
         GramJob R{};
         R.na = na; R.nb = nb; R.nchunks = gp.rc; R.part = P.part; R.C = C; R.ldc = ldc;
         rj.push_back(R);
@@ -1808,8 +1815,9 @@ int plan_wave(SplitStaged& S, SWave& W) {
     auto flush_gram = [&]() {
         flush_prepare();
         push(kSGram, gj, gc);
+        push(kSGram16, gj16, gc16);
         push(kSReduce, rj, rc2);
-        gj.clear(); gc.clear(); rj.clear(); rc2.clear();
+        gj.clear(); gc.clear(); gj16.clear(); gc16.clear(); rj.clear(); rc2.clear();
     };
 
     std::vector<SmallJob> smj;
@@ -2139,17 +2147,19 @@ int enqueue_wave(SplitStaged& S, SWave& W, cudaStream_t st) {
                                                             L.njobs);
                 ++g_launch_count;
                 break;
-            case kSGram: {
+            case kSGram:
+            case kSGram16: {
                 const auto* J = reinterpret_cast<const SplitGramJob*>(jb + L.job_off);
-                if (KD == 6)
-                    gram_tc_kernel<6, 6, true><<<items, NTHREADS, SmemLayout<32, 6>::BYTES, st>>>(
-                        none, none, none, g0, J, pre, L.njobs);
-                else if (gram_a_planes(KD) == 6)
-                    gram_tc_kernel<7, 6, true><<<items, NTHREADS, SmemLayout<32, 7>::BYTES, st>>>(
-                        none, none, none, g0, J, pre, L.njobs);
-                else
-                    gram_tc_kernel<7, 7, true><<<items, NTHREADS, SmemLayout<32, 7>::BYTES, st>>>(
-                        none, none, none, g0, J, pre, L.njobs);
+                const int ka = gram_a_planes(KD);
+#define BCGS_GRAMB(NBT, KDT, KAT)                                                                              \
+    gram_tc_kernel<NBT, KDT, KAT, true><<<items, NTHREADS, SmemLayout<NBT, KDT>::BYTES, st>>>(none, none, none, \
+                                                                                            g0, J, pre, L.njobs)
+                if (L.kind == kSGram16) {
+                    if (KD == 6) BCGS_GRAMB(16, 6, 6); else if (ka == 6) BCGS_GRAMB(16, 7, 6); else BCGS_GRAMB(16, 7, 7);
+                } else {
+                    if (KD == 6) BCGS_GRAMB(32, 6, 6); else if (ka == 6) BCGS_GRAMB(32, 7, 6); else BCGS_GRAMB(32, 7, 7);
+                }
+#undef BCGS_GRAMB
                 ++g_launch_count;
                 break;
             }
@@ -2296,9 +2306,12 @@ int split_staged_create(int count, const int* m, const int* n, const int* s, dou
     int rc = fill_smats(*S, count, m, n, s, dX, ldX, dR, ldR, dstatus);
     if (rc) { free_staged(S); return rc; }
     // Shared-memory limits of the batched kernels on this device.
-    rc = set_smem(gram_tc_kernel<6, 6, true>, SmemLayout<32, 6>::BYTES);
-    if (!rc) rc = set_smem(gram_tc_kernel<7, 7, true>, SmemLayout<32, 7>::BYTES);
-    if (!rc) rc = set_smem(gram_tc_kernel<7, 6, true>, SmemLayout<32, 7>::BYTES);
+    rc = set_smem(gram_tc_kernel<32, 6, 6, true>, SmemLayout<32, 6>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<32, 7, 7, true>, SmemLayout<32, 7>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<32, 7, 6, true>, SmemLayout<32, 7>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<16, 6, 6, true>, SmemLayout<16, 6>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<16, 7, 7, true>, SmemLayout<16, 7>::BYTES);
+    if (!rc) rc = set_smem(gram_tc_kernel<16, 7, 6, true>, SmemLayout<16, 7>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<32, 6, true>, SmemLayout<32, 6>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<32, 7, true>, SmemLayout<32, 7>::BYTES);
     if (!rc) rc = set_smem(update_tc_kernel<16, 6, true>, SmemLayout<16, 6>::BYTES);
