@@ -413,16 +413,27 @@ def run_ours(args, rank, world, local_rank):
             return times, {key: round(sum(t[key] for t in timelines) / len(timelines), 1) for key in timelines[0]}
 
         orth.set_host_precision(prec)
-        hx, hr = orth.HostBuffer(m * n * 8), orth.HostBuffer(n * n * 8)
-        times, timeline = host_leg(hx.array((m, n)), hr.array((n, n)), args.e2e_steps)
-        hx.close()
-        hr.close()
+        try:
+            hx, hr = orth.HostBuffer(m * n * 8), orth.HostBuffer(n * n * 8)
+            Xh, Rh = hx.array((m, n)), hr.array((n, n))
+            buf_kind = "page-locked huge-page buffers from orth_gb300_host_alloc"
+        except RuntimeError:
+            # Several ranks on one host may not get that much page-locked memory:
+            # the CUDA allocator's page-locked buffers instead.
+            hx = hr = None
+            Xh = torch.empty((n, m), dtype=torch.float64, pin_memory=True).numpy().T
+            Rh = torch.zeros((n, n), dtype=torch.float64, pin_memory=True).numpy().T
+            buf_kind = "cudaHostAlloc buffers (orth_gb300_host_alloc failed)"
+        times, timeline = host_leg(Xh, Rh, args.e2e_steps)
+        del Xh, Rh
+        if hx is not None:
+            hx.close()
+            hr.close()
         e2e_ms = max_over_ranks(sum(times) / len(times), world, dev)
         e2e = {"value": round(e2e_ms, 3), "unit": "ms", "samples_ms": [round(x, 1) for x in times],
                "timeline_ms": timeline,
                "h2d_bytes_per_step": m * n * 8, "d2h_bytes_per_step": m * n * 8 + n * n * 8,
-               "path": f"orth.h {variant} (host pointers: page-locked huge-page buffers from "
-                       f"orth_gb300_host_alloc), {prec_name}"}
+               "path": f"orth.h {variant} (host pointers: {buf_kind}), {prec_name}"}
         if args.e2e_cuda_host_alloc:
             Xc = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
             Rc = torch.zeros((n, n), dtype=torch.float64, pin_memory=True)
