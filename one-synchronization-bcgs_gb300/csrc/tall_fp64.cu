@@ -19,26 +19,34 @@
 namespace bcgs {
 
 namespace {
-constexpr int GT_A = 64;    // C rows per CTA (single-matrix form)
-constexpr int GT_B = 32;    // C columns per CTA (single-matrix form)
-constexpr int GT_R = 32;    // chunk row ranges are multiples of this
-constexpr int GT_THREADS = 256;
+// Single-matrix Gram: one CTA per 16-column strip of A x 32 columns of B x row
+// chunk, so na (a multiple of s) wastes no work on zero padding.
+constexpr int GS_A = 16;            // C rows per CTA
+constexpr int GS_B = 32;            // C columns per CTA
+constexpr int GS_R = 16;            // X rows per shared-memory sub-tile
+constexpr int GS_CTAS_PER_SM = 16;  // resident strip CTAs per SM (64 registers, 7 KB)
+constexpr int GT_R = 32;            // chunk row ranges are multiples of this
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// Gram partials. CTA tile: GA = 2048/TB rows of C (columns of A) x TB columns of C
-// (columns of B), TB in {8, 16, 32}; 256 threads, each owning a 4 x 2 register
-// tile. The CTA walks a contiguous row range of X in sub-tiles of GR = TB rows
-// staged in shared memory. Partial sums go to part[chunk][i + j * na]
-// (column-major na x nb per chunk). Every entry is a sequential FMA chain over the
-// rows of the chunk in order, so the result does not depend on TB.
+// Gram partials. CTA tile: GA rows of C (columns of A) x TB columns of C (columns
+// of B); (GA/4) x (TB/2) threads, each owning a 4 x 2 register tile. The CTA walks
+// a contiguous row range of X in sub-tiles of GR rows staged in shared memory.
+// Partial sums go to part[chunk][i + j * na] (column-major na x nb per chunk).
+// Every entry is a sequential FMA chain over the rows of the chunk in order, so
+// the result depends on the chunking only, not on GA, TB or GR.
 // ---------------------------------------------------------------------------
-template <int TB>
-struct GramPanel {
-    static constexpr int GA = 2048 / TB;   // C rows per CTA
-    static constexpr int GR = TB;          // X rows per shared-memory sub-tile
-    static constexpr int SMEM = GR * (GA + 1) + GR * (TB + 1);   // doubles
+template <int GA_, int TB_, int GR_>
+struct GramTile {
+    static constexpr int GA = GA_, TB = TB_, GR = GR_;
+    static constexpr int NT = (GA / 4) * (TB / 2);                // threads
+    static constexpr int SMEM = GR * (GA + 1) + GR * (TB + 1);    // doubles
 };
+// Batched form: 256 threads, GA = 2048 / TB, TB in {8, 16, 32}.
+template <int TB>
+using GramPanel = GramTile<2048 / TB, TB, TB>;
+using GramStrip = GramTile<GS_A, GS_B, GS_R>;
+static_assert(GramStrip::NT == 64, "strip CTA is two warps");
 constexpr int kGramSmemMax = GramPanel<32>::SMEM > GramPanel<8>::SMEM
                                  ? (GramPanel<32>::SMEM > GramPanel<16>::SMEM ? GramPanel<32>::SMEM
                                                                               : GramPanel<16>::SMEM)
@@ -46,15 +54,17 @@ constexpr int kGramSmemMax = GramPanel<32>::SMEM > GramPanel<8>::SMEM
                                                                              : GramPanel<16>::SMEM);
 
 // The tile at C rows ia0.., C columns jb0.., rows [r_begin, r_end) of X, written to
-// `out` (na x nb, ld na). 256 threads; sm holds GramPanel<TB>::SMEM doubles.
-// SEG > 0: every SEG sub-tiles of GR rows the running sums are added to a total
-// and restarted, so no FMA chain is longer than SEG * GR rows however long the
-// row range is (SEG = 0: one chain over the range).
-template <int TB, int SEG = 0>
+// `out` (na x nb, ld na). Tile::NT threads; sm holds Tile::SMEM doubles.
+// SEGR > 0: every SEGR rows the running sums are added to a total and restarted,
+// so no FMA chain is longer than SEGR rows however long the row range is
+// (SEGR = 0: one chain over the range).
+template <class Tile, int SEGR = 0>
 __device__ __forceinline__ void gram_partial_body(const double* __restrict__ X, i64 ld, int a0, int na, int b0,
                                                   int nb, i64 r_begin, i64 r_end, int ia0, int jb0,
                                                   double* __restrict__ out, double* __restrict__ sm) {
-    constexpr int GA = GramPanel<TB>::GA, GR = GramPanel<TB>::GR, NT = 256;
+    constexpr int GA = Tile::GA, TB = Tile::TB, GR = Tile::GR, NT = Tile::NT;
+    constexpr int SEG = SEGR / GR;  // sub-tiles per segment
+    static_assert(SEGR % GR == 0, "segments are whole sub-tiles");
     constexpr int TI = GA / 4;      // threads along C rows -> 4 rows each
     double (*sA)[GA + 1] = reinterpret_cast<double (*)[GA + 1]>(sm);
     double (*sB)[TB + 1] = reinterpret_cast<double (*)[TB + 1]>(sm + GR * (GA + 1));
@@ -122,28 +132,28 @@ __device__ __forceinline__ void gram_partial_body(const double* __restrict__ X, 
     }
 }
 
-__global__ void __launch_bounds__(GT_THREADS, 4)
+__global__ void __launch_bounds__(GramStrip::NT, GS_CTAS_PER_SM)
 gram_fp64_partial(const double* __restrict__ X, i64 ld, i64 m, int a0, int na, int b0, int nb,
                   i64 rows_per_chunk, double* __restrict__ part) {
-    __shared__ double sm[GramPanel<GT_B>::SMEM];
+    __shared__ double sm[GramStrip::SMEM];
     const int chunk = blockIdx.x;
     const i64 r_begin = (i64)chunk * rows_per_chunk;
     const i64 r_end = min(m, r_begin + rows_per_chunk);
-    gram_partial_body<GT_B>(X, ld, a0, na, b0, nb, r_begin, r_end, blockIdx.y * GT_A, blockIdx.z * GT_B,
-                            part + (i64)chunk * na * nb, sm);
+    gram_partial_body<GramStrip>(X, ld, a0, na, b0, nb, r_begin, r_end, blockIdx.y * GS_A, blockIdx.z * GS_B,
+                                 part + (i64)chunk * na * nb, sm);
 }
 
 // The same over chunks of rows_per_chunk rows, each summed in segments of
 // 256 rows (the row-sharded path's long chunks).
-__global__ void __launch_bounds__(GT_THREADS, 4)
+__global__ void __launch_bounds__(GramStrip::NT, GS_CTAS_PER_SM)
 gram_fp64_partial_seg(const double* __restrict__ X, i64 ld, i64 m, int a0, int na, int b0, int nb,
                       i64 rows_per_chunk, double* __restrict__ part) {
-    __shared__ double sm[GramPanel<GT_B>::SMEM];
+    __shared__ double sm[GramStrip::SMEM];
     const int chunk = blockIdx.x;
     const i64 r_begin = (i64)chunk * rows_per_chunk;
     const i64 r_end = min(m, r_begin + rows_per_chunk);
-    gram_partial_body<GT_B, 256 / GramPanel<GT_B>::GR>(X, ld, a0, na, b0, nb, r_begin, r_end, blockIdx.y * GT_A,
-                                                        blockIdx.z * GT_B, part + (i64)chunk * na * nb, sm);
+    gram_partial_body<GramStrip, 256>(X, ld, a0, na, b0, nb, r_begin, r_end, blockIdx.y * GS_A,
+                                      blockIdx.z * GS_B, part + (i64)chunk * na * nb, sm);
 }
 
 // Fixed-order sum over chunks: out[i + j*ldo] = sum_{c=0}^{nchunks-1} part[c][i + j*na].
@@ -170,9 +180,12 @@ int gram_chunks_fp64(i64 m, int na, int nb, int num_sms) {
         const i64 c = ceil_div(m, g_gram_chunk_rows);
         return (int)(c < 1 ? 1 : c);
     }
-    const i64 tiles = ceil_div(na, GT_A) * ceil_div(nb, GT_B);
-    // About four CTAs per SM in total, each with at least 256 rows.
-    i64 want = ceil_div(4LL * num_sms, tiles);
+    // One wave: the most chunks whose strip CTAs all fit on the SMs at once, so
+    // every SM gets the same number of equal CTAs (within one), each with at
+    // least 256 rows. The FP64 pipe is saturated by two resident CTAs per SM;
+    // what costs time is an SM holding more CTAs than the others.
+    const i64 ctas_per_chunk = ceil_div(na, GS_A) * ceil_div(nb, GS_B);
+    i64 want = (i64)GS_CTAS_PER_SM * num_sms / ctas_per_chunk;
     i64 max_by_rows = ceil_div(m, 256);
     i64 c = want < max_by_rows ? want : max_by_rows;
     if (c < 1) c = 1;
@@ -185,8 +198,8 @@ int launch_gram_fp64(const double* X, i64 ld, i64 m, int a0, int na, int b0, int
     if (na <= 0 || nb <= 0) return 0;
     i64 rows_per_chunk = ceil_div(m, nchunks);
     rows_per_chunk = ceil_div(rows_per_chunk, GT_R) * GT_R;
-    dim3 grid((unsigned)nchunks, (unsigned)ceil_div(na, GT_A), (unsigned)ceil_div(nb, GT_B));
-    gram_fp64_partial<<<grid, GT_THREADS, 0, st>>>(X, ld, m, a0, na, b0, nb, rows_per_chunk, part);
+    dim3 grid((unsigned)nchunks, (unsigned)ceil_div(na, GS_A), (unsigned)ceil_div(nb, GS_B));
+    gram_fp64_partial<<<grid, GramStrip::NT, 0, st>>>(X, ld, m, a0, na, b0, nb, rows_per_chunk, part);
     i64 total = (i64)na * nb;
     int blocks = (int)ceil_div(total, 256);
     if (blocks > 4 * 152) blocks = 4 * 152;
@@ -201,8 +214,8 @@ int launch_gram_partials_fp64(const double* X, i64 ld, i64 m, int a0, int na, in
     if (na <= 0 || nb <= 0 || m <= 0) return 0;
     if (rows <= 0 || rows % GT_R != 0) return (int)cudaErrorInvalidValue;
     const i64 nchunks = ceil_div(m, rows);
-    dim3 grid((unsigned)nchunks, (unsigned)ceil_div(na, GT_A), (unsigned)ceil_div(nb, GT_B));
-    gram_fp64_partial_seg<<<grid, GT_THREADS, 0, st>>>(X, ld, m, a0, na, b0, nb, rows, part);
+    dim3 grid((unsigned)nchunks, (unsigned)ceil_div(na, GS_A), (unsigned)ceil_div(nb, GS_B));
+    gram_fp64_partial_seg<<<grid, GramStrip::NT, 0, st>>>(X, ld, m, a0, na, b0, nb, rows, part);
     g_launch_count += 1;
     return (int)cudaGetLastError();
 }
@@ -337,7 +350,7 @@ int launch_update_fp64(double* X, i64 ld, i64 m, int q0, int K, int c0, int nc,
 // ---------------------------------------------------------------------------
 int gram_batched_panel_rows(int tb) { return 2048 / tb; }
 
-__global__ void __launch_bounds__(GT_THREADS, 4)
+__global__ void __launch_bounds__(256, 4)
 gram_partial_batched(const GramJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
     __shared__ double sm[kGramSmemMax];
     const int j = batched_job_of(prefix, njobs, blockIdx.x);
@@ -349,14 +362,13 @@ gram_partial_batched(const GramJob* __restrict__ jobs, const int* __restrict__ p
     const i64 r_begin = (i64)chunk * J.rows_per_chunk;
     const i64 r_end = min(J.m, r_begin + J.rows_per_chunk);
     double* out = J.part + (i64)chunk * J.na * J.nb;
+    const int ia0 = ia * (2048 / J.tb);
     if (J.tb == 8)
-        gram_partial_body<8>(J.X, J.ld, 0, J.na, J.b0, J.nb, r_begin, r_end, ia * GramPanel<8>::GA, jb * 8, out, sm);
+        gram_partial_body<GramPanel<8>>(J.X, J.ld, 0, J.na, J.b0, J.nb, r_begin, r_end, ia0, jb * 8, out, sm);
     else if (J.tb == 16)
-        gram_partial_body<16>(J.X, J.ld, 0, J.na, J.b0, J.nb, r_begin, r_end, ia * GramPanel<16>::GA, jb * 16, out,
-                              sm);
+        gram_partial_body<GramPanel<16>>(J.X, J.ld, 0, J.na, J.b0, J.nb, r_begin, r_end, ia0, jb * 16, out, sm);
     else
-        gram_partial_body<32>(J.X, J.ld, 0, J.na, J.b0, J.nb, r_begin, r_end, ia * GramPanel<32>::GA, jb * 32, out,
-                              sm);
+        gram_partial_body<GramPanel<32>>(J.X, J.ld, 0, J.na, J.b0, J.nb, r_begin, r_end, ia0, jb * 32, out, sm);
 }
 
 // Same summation order as gram_reduce: each entry sums the chunks in order.
@@ -389,7 +401,7 @@ update_batched(const UpdJob* __restrict__ jobs, const int* __restrict__ prefix, 
 
 int launch_gram_partial_batched(const GramJob* jobs, const int* prefix, int njobs, int items, cudaStream_t st) {
     if (items <= 0) return 0;
-    gram_partial_batched<<<(unsigned)items, GT_THREADS, 0, st>>>(jobs, prefix, njobs);
+    gram_partial_batched<<<(unsigned)items, 256, 0, st>>>(jobs, prefix, njobs);
     g_launch_count += 1;
     return (int)cudaGetLastError();
 }
