@@ -196,8 +196,24 @@ int orth_gb300_accuracy_dev(int m, int n, const double *dX, long long ldX, const
                             double out[3]);
 
 /*
- * Rows per chunk of the FP64 Gram's fixed-order reduction (0 = the default policy,
- * about four CTAs per SM). Results depend on the chunking only through the order
+ * The split form's digit planes of a matrix, for tests of the slicing: each column
+ * c of X (m x n, ldX >= m) is scaled by 2^-e_c, e_c the exponent with max |X[:, c]|
+ * < 2^e_c (Inf and NaN ignored; 0 for a zero column), rounded to the fixed point
+ * V = round(x * 2^(8 planes - 1 - e_c)) (half away from zero) and split into
+ * `planes` (6 or 7) balanced base-256 digits d_0 (most significant) .. in
+ * [-128, 128], stored as BF16 bits. dDigits (planes * ceil(m/64) * 64 * n
+ * unsigned shorts) receives them in the store's layout: digit i of X[r, c] at
+ * ((i * ceil(m/64) + r/64) * n + c) * 64 + r % 64, rows past m as digits of zero;
+ * dExp[n] receives e_c. Synchronizes the stream. Returns 0, 2 (invalid arguments,
+ * or n > 65535) or 3 (CUDA failure).
+ */
+int orth_gb300_split_slice_dev(long long m, int n, const double *dX, long long ldX, int planes,
+                               unsigned short *dDigits, int *dExp, void *stream);
+
+/*
+ * Rows per chunk of the FP64 Gram's fixed-order reduction (0 = the default policy:
+ * the most chunks whose 16-column strip CTAs all fit on the SMs in one wave, at
+ * least 256 rows each). Results depend on the chunking only through the order
  * of the final sum; a batched plan with the same chunk rows reproduces the
  * single-matrix results bit for bit.
  */

@@ -120,6 +120,9 @@ def load(path: str | None = None):
                                             ctypes.POINTER(ctypes.c_double)]
     lib.orth_gb300_accuracy_dev.restype = ctypes.c_int
     lib.orth_gb300_set_gram_chunk_rows.argtypes = [ctypes.c_longlong]
+    lib.orth_gb300_split_slice_dev.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong,
+                                               ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.orth_gb300_split_slice_dev.restype = ctypes.c_int
     lib.orth_gb300_poison_shared_memory.argtypes = [ctypes.c_ulonglong, ctypes.c_void_p]
     lib.orth_gb300_poison_shared_memory.restype = ctypes.c_int
     lib.orth_gb300_timeout_probe.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
@@ -415,6 +418,15 @@ def accuracy_dev(m: int, n: int, x_ptr: int, ldx: int, q_ptr: int, ldq: int, r_p
                                             ctypes.c_void_p(e_ptr or None), lde or n, ctypes.c_void_p(stream),
                                             out))
     return rc, float(out[0]), float(out[1]), float(out[2])
+
+
+def split_slice_dev(m: int, n: int, x_ptr: int, ldx: int, planes: int, digits_ptr: int, exp_ptr: int,
+                    stream: int = 0) -> int:
+    """The split form's BF16 digit planes of X (m x n, ld ldx) in the digit store's
+    layout, and each column's scale exponent (orth_gb300_split_slice_dev)."""
+    return int(load().orth_gb300_split_slice_dev(m, n, ctypes.c_void_p(x_ptr), ldx, planes,
+                                                 ctypes.c_void_p(digits_ptr), ctypes.c_void_p(exp_ptr),
+                                                 ctypes.c_void_p(stream)))
 
 
 def poison_shared_memory(bits: int = 0x7FF8DEADBEEF0001, stream: int = 0) -> int:

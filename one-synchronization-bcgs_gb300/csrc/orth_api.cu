@@ -1541,6 +1541,18 @@ int orth_gb300_split_batch_plan(int count, const int* m, const int* n, const int
     return S;
 }
 
+int orth_gb300_split_slice_dev(long long m, int n, const double* dX, long long ldX, int planes,
+                               unsigned short* dDigits, int* dExp, void* stream) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (m < 1 || n < 1 || n > 65535 || !dX || !dDigits || !dExp || ldX < m || (planes != 6 && planes != 7)) return 2;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (init_ctx()) return 3;
+    if (g_ctx.metric.ensure((size_t)n * sizeof(unsigned long long))) return 3;
+    int rc = split_slice_columns(dX, ldX, m, n, planes, dDigits, dExp, g_ctx.metric.as<unsigned long long>(), st);
+    if (!rc) rc = (int)cudaStreamSynchronize(st);
+    return rc ? 3 : 0;
+}
+
 void orth_gb300_set_gram_chunk_rows(long long rows) {
     std::lock_guard<std::mutex> lock(g_mu);
     g_gram_chunk_rows = rows > 0 ? rows : 0;

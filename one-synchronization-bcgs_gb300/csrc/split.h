@@ -23,6 +23,11 @@ int split_prepare(int c_end, cudaStream_t st);
 int split_digits();
 // Columns [c0, c0+nc) of X were rewritten outside the split kernels.
 void split_mark_stale(int c0, int nc);
+// The digit planes of all n columns of X (m x n, ld) in the store's layout
+// ([plane][64-row chunk][column][64 rows], ceil(m / 64) chunks), each column's
+// scale exponent into cexp[n]; cmax: n words of scratch. kd: 6 or 7.
+int split_slice_columns(const double* X, i64 ld, i64 m, int n, int kd, unsigned short* digits, int* cexp,
+                        unsigned long long* cmax, cudaStream_t st);
 // Reads (and waits for) the split kernels' error word: 0, or the code of a wait
 // that ran out.
 int split_error_word(int* out, cudaStream_t st);

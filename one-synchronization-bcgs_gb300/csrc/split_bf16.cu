@@ -175,9 +175,44 @@ __global__ void colmax_kernel(const double* __restrict__ X, i64 ld, i64 m, int c
     colmax_body(X, ld, m, c0 + (int)blockIdx.y, (int)blockIdx.x, cmax);
 }
 
+// BF16 sum of two pairs of BF16 values (exact here: integers of at most 8 bits).
+__device__ __forceinline__ uint32_t bf16x2_add(uint32_t a, uint32_t b) {
+    uint32_t d;
+    asm("add.rn.bf16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+
+// The digits of two values of one column (scale exponent e), packed: word i holds
+// the BF16 bits of digit i of xa in its low half and of xb in its high half, the
+// same bits split_digits + bf16_bits_of_int give. A low digit is byte k of
+// V + bias, b = d + 128; with lo = b & 127 and b7 = b & 128, the BF16 words
+// 0x4300 | lo (= 128 + lo) and 0xC380 ^ b7 (= -256 + b7) add exactly to
+// lo + b7 - 128 = d, two digits per byte permute, two logic operations and one
+// BF16x2 add.
+template <int KD>
+__device__ __forceinline__ void split_digits_pair(double xa, double xb, int e, uint32_t* w) {
+    constexpr unsigned long long kBias = 0x8080808080808080ULL >> (8 * (8 - (KD - 1)));
+    const unsigned long long va = (unsigned long long)(fixed_point_of<KD>(xa, e) + (long long)kBias);
+    const unsigned long long vb = (unsigned long long)(fixed_point_of<KD>(xb, e) + (long long)kBias);
+    const uint32_t alo = (uint32_t)va, ahi = (uint32_t)(va >> 32);
+    const uint32_t blo = (uint32_t)vb, bhi = (uint32_t)(vb >> 32);
+#pragma unroll
+    for (int i = 1; i < KD; ++i) {
+        const int k = KD - 1 - i;   // byte of V + bias holding digit i
+        const uint32_t p = k < 4 ? __byte_perm(alo, blo, (unsigned)(k | ((4 + k) << 8)))
+                                 : __byte_perm(ahi, bhi, (unsigned)((k - 4) | (k << 8)));
+        w[i] = bf16x2_add((p & 0x007F007Fu) | 0x43004300u, (p & 0x00800080u) ^ 0xC380C380u);
+    }
+    const int d0a = (int)((long long)va >> (8 * (KD - 1)));
+    const int d0b = (int)((long long)vb >> (8 * (KD - 1)));
+    w[0] = (uint32_t)bf16_bits_of_int(d0a) | ((uint32_t)bf16_bits_of_int(d0b) << 16);
+}
+
 // Slice columns [c0, c0+nc) of X into the digit store. A CTA handles 128 rows x
-// 16 columns (grid: row tiles x column groups), one row per thread: 16 coalesced
-// column loads and the digits, staged in shared memory as [plane][64-row
+// 16 columns (grid: row tiles x column groups); thread t makes the digits of rows
+// 2u, 2u + 1 (u = t % 64) for 8 of the columns, from one 16-byte load per column
+// where the columns start on 16-byte boundaries, two digits per 32-bit word
+// (split_digits_pair). The digits are staged in shared memory as [plane][64-row
 // half][column][64 rows]. That is the store's own layout: for one plane and one
 // 64-row chunk, the 16 columns' runs of 64 rows are one contiguous 2 KB block of
 // HBM. A tile of 128 whole rows leaves as 2 KD bulk copies (128 bytes per valid
@@ -188,21 +223,33 @@ __device__ __forceinline__ void slice_body(const double* __restrict__ X, i64 ld,
                                            const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
                                            unsigned short* __restrict__ colstore, i64 nrc, int bx, int by) {
     constexpr int CG = 16;                   // columns per CTA
-    __shared__ __align__(128) unsigned short sdig[KD][2][CG][64];
+    constexpr int CT = CG / 2;               // columns per thread
+    __shared__ __align__(128) uint32_t sw[KD][2][CG][32];
+    typedef unsigned short Run[2][CG][64];
+    const Run* sdig = reinterpret_cast<const Run*>(&sw[0][0][0][0]);
     const int t = threadIdx.x;
+    const int u = t & 63;                    // rows 2u, 2u + 1 of the tile
+    const int jt = (t >> 6) * CT;            // the thread's first column of the group
     const int g = by * CG;                   // first column of this group (relative to c0)
     const i64 r0 = (i64)bx * 128;
-    const i64 r = r0 + t;
+    const i64 r = r0 + 2 * u;
     if (bx == 0 && t < CG && g + t < nc) cexp[c0 + g + t] = scale_exp(cmax[c0 + g + t]);
-    double x[CG];
+    const bool pair = ((reinterpret_cast<uintptr_t>(X) | (uintptr_t)(ld * 8)) & 15) == 0 && r + 1 < m;
+    double2 x[CT];
 #pragma unroll
-    for (int j = 0; j < CG; ++j) x[j] = (g + j < nc && r < m) ? X[r + (i64)(c0 + g + j) * ld] : 0.0;
+    for (int j = 0; j < CT; ++j) {
+        const double* p = X + r + (i64)(c0 + g + jt + j) * ld;
+        if (g + jt + j >= nc) x[j] = make_double2(0.0, 0.0);
+        else if (pair) x[j] = *reinterpret_cast<const double2*>(p);
+        else x[j] = make_double2(r < m ? p[0] : 0.0, r + 1 < m ? p[1] : 0.0);
+    }
 #pragma unroll
-    for (int j = 0; j < CG; ++j) {
-        int d[KD];
-        split_digits<KD>(x[j], g + j < nc ? scale_exp(cmax[c0 + g + j]) : 0, d);
+    for (int j = 0; j < CT; ++j) {
+        const int c = g + jt + j;
+        uint32_t w[KD];
+        split_digits_pair<KD>(x[j].x, x[j].y, c < nc ? scale_exp(cmax[c0 + c]) : 0, w);
 #pragma unroll
-        for (int i = 0; i < KD; ++i) sdig[i][t >> 6][j][t & 63] = bf16_bits_of_int(d[i]);
+        for (int i = 0; i < KD; ++i) sw[i][u >> 5][jt + j][u & 31] = w[i];
     }
     // A tile whose 128 rows all lie below m leaves as bulk copies of its valid
     // columns (ncols x 128 bytes per plane and 64-row half: the store keeps a
@@ -238,12 +285,13 @@ __device__ __forceinline__ void slice_body(const double* __restrict__ X, i64 ld,
 }
 
 template <int KD>
-__global__ void __launch_bounds__(128, 6)
+__global__ void __launch_bounds__(128, 7)
 slice_kernel(const double* __restrict__ X, i64 ld, i64 m, int n, int c0, int nc,
              const unsigned long long* __restrict__ cmax, int* __restrict__ cexp,
              unsigned short* __restrict__ colstore, i64 nrc) {
     slice_body<KD>(X, ld, m, n, c0, nc, cmax, cexp, colstore, nrc, (int)blockIdx.x, (int)blockIdx.y);
 }
+
 
 // Right-hand factor of the update, scaled: Bp[c + j*ldb] for c < K + nc, j < nc:
 //   c <  K : -(S T^{-1})[c, j] * 2^{cexp[c]}      (or -S[c, j] * 2^{cexp[c]} if T is null)
@@ -1232,6 +1280,11 @@ size_t layout_bytes(i64 m, int n, int s, int num_sms, Plan* out, char* base) {
     return cv.off + 1024;
 }
 
+template <class K>
+int set_smem(K kernel, int bytes) {
+    return smem_attr((const void*)kernel, bytes);
+}
+
 int ensure_fresh(int c_begin, int c_end, cudaStream_t st) {
     Plan& P = cur_plan();
     int c = c_begin;
@@ -1257,11 +1310,6 @@ int ensure_fresh(int c_begin, int c_end, cudaStream_t st) {
         c = e;
     }
     return (int)cudaGetLastError();
-}
-
-template <class K>
-int set_smem(K kernel, int bytes) {
-    return smem_attr((const void*)kernel, bytes);
 }
 
 }  // namespace
@@ -1361,6 +1409,25 @@ int split_error_word(int* out, cudaStream_t st) {
 int split_last_error() { return g_last_split_error; }
 
 int split_prepare(int c_end, cudaStream_t st) { return ensure_fresh(0, c_end, st); }
+
+int split_slice_columns(const double* X, i64 ld, i64 m, int n, int kd, unsigned short* digits, int* cexp,
+                        unsigned long long* cmax, cudaStream_t st) {
+    if ((kd != 6 && kd != 7) || m < 1 || n < 1 || n > 65535) return (int)cudaErrorInvalidValue;
+    const i64 nrc = ceil_div(m, 64);
+    // The slicing writes rows below m only; the rows past m in the last chunk
+    // read as zero, as in the store.
+    int rc = zero_async(digits, (size_t)kd * nrc * 64 * n * sizeof(unsigned short), st);
+    if (!rc) rc = zero_async(cmax, (size_t)n * sizeof(unsigned long long), st);
+    if (rc) return rc;
+    colmax_kernel<<<dim3((unsigned)ceil_div(m, 4096), (unsigned)n), 256, 0, st>>>(X, ld, m, 0, cmax);
+    const dim3 sgrid((unsigned)ceil_div(m, 128), (unsigned)ceil_div(n, 16));
+    if (kd == 6)
+        slice_kernel<6><<<sgrid, 128, 0, st>>>(X, ld, m, n, 0, n, cmax, cexp, digits, nrc);
+    else
+        slice_kernel<7><<<sgrid, 128, 0, st>>>(X, ld, m, n, 0, n, cmax, cexp, digits, nrc);
+    g_launch_count += 2;
+    return (int)cudaGetLastError();
+}
 
 int split_digits() { return cur_plan().kd; }
 

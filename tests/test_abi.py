@@ -100,3 +100,11 @@ def test_host_buffer_argument_checks(lib):
     assert lib.orth_gb300_host_alloc(ctypes.c_size_t(64), None) == 2
     assert lib.orth_gb300_host_free(None) == 0
     assert lib.orth_gb300_host_free(ctypes.c_void_p(0x12345000)) == 2   # not from orth_gb300_host_alloc
+
+
+def test_split_slice_argument_checks(lib):
+    """orth_gb300_split_slice_dev rejects bad arguments before any CUDA call."""
+    assert orth.split_slice_dev(0, 4, 0, 1, 7, 0, 0) == 2          # m < 1
+    assert orth.split_slice_dev(16, 4, 0, 16, 7, 0, 0) == 2         # null buffers
+    assert orth.split_slice_dev(16, 4, 0x1000, 8, 7, 0x1000, 0x1000) == 2   # ldX < m
+    assert orth.split_slice_dev(16, 4, 0x1000, 16, 5, 0x1000, 0x1000) == 2  # planes not 6 or 7
