@@ -19,9 +19,9 @@
 // (orth_gb300_set_gram_chunk_rows) the results are bit-identical.
 //
 // Tuning: per block size s, the Gram's B-panel width (8, 16 or 32 columns; the
-// A-panel holds 2048 / width columns) and the rows per Gram chunk (4096 ... 32768)
-// are picked by timing each candidate on a representative Gram stage of that
-// class's matrices.
+// A-panel holds 512 / width columns, 64 threads per CTA) and the rows per Gram
+// chunk (4096 ... 32768) are picked by timing each candidate on a representative
+// Gram stage of that class's matrices.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>

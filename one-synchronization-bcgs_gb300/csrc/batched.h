@@ -20,7 +20,7 @@ struct GramJob {
     double* part;   // nchunks * na * nb doubles
     double* C;
     int ldc;
-    int tb;         // B-panel width: 8, 16 or 32 (A-panel height 2048 / tb)
+    int tb;         // B-panel width: 8, 16 or 32 (A-panel height 512 / tb)
     int tilesA, tilesB;
 };
 

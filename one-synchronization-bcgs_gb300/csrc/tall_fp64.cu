@@ -42,11 +42,13 @@ struct GramTile {
     static constexpr int NT = (GA / 4) * (TB / 2);                // threads
     static constexpr int SMEM = GR * (GA + 1) + GR * (TB + 1);    // doubles
 };
-// Batched form: 256 threads, GA = 2048 / TB, TB in {8, 16, 32}.
+// Batched form: 64 threads, GA = 512 / TB, TB in {8, 16, 32} (B panels of 2s
+// columns for s = 4, 8, 16 against A strips of 64, 32 or 16 columns).
 template <int TB>
-using GramPanel = GramTile<2048 / TB, TB, TB>;
+using GramPanel = GramTile<512 / TB, TB, 16>;
 using GramStrip = GramTile<GS_A, GS_B, GS_R>;
-static_assert(GramStrip::NT == 64, "strip CTA is two warps");
+static_assert(GramStrip::NT == 64 && GramPanel<8>::NT == 64 && GramPanel<16>::NT == 64 && GramPanel<32>::NT == 64,
+              "strip CTAs are two warps");
 constexpr int kGramSmemMax = GramPanel<32>::SMEM > GramPanel<8>::SMEM
                                  ? (GramPanel<32>::SMEM > GramPanel<16>::SMEM ? GramPanel<32>::SMEM
                                                                               : GramPanel<16>::SMEM)
@@ -348,9 +350,9 @@ int launch_update_fp64(double* X, i64 ld, i64 m, int q0, int K, int c0, int nc,
 // ---------------------------------------------------------------------------
 // Batched forms: one launch over many matrices' jobs (batched.h).
 // ---------------------------------------------------------------------------
-int gram_batched_panel_rows(int tb) { return 2048 / tb; }
+int gram_batched_panel_rows(int tb) { return 512 / tb; }
 
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(64, GS_CTAS_PER_SM)
 gram_partial_batched(const GramJob* __restrict__ jobs, const int* __restrict__ prefix, int njobs) {
     __shared__ double sm[kGramSmemMax];
     const int j = batched_job_of(prefix, njobs, blockIdx.x);
@@ -362,7 +364,7 @@ gram_partial_batched(const GramJob* __restrict__ jobs, const int* __restrict__ p
     const i64 r_begin = (i64)chunk * J.rows_per_chunk;
     const i64 r_end = min(J.m, r_begin + J.rows_per_chunk);
     double* out = J.part + (i64)chunk * J.na * J.nb;
-    const int ia0 = ia * (2048 / J.tb);
+    const int ia0 = ia * (512 / J.tb);
     if (J.tb == 8)
         gram_partial_body<GramPanel<8>>(J.X, J.ld, 0, J.na, J.b0, J.nb, r_begin, r_end, ia0, jb * 8, out, sm);
     else if (J.tb == 16)
@@ -401,7 +403,7 @@ update_batched(const UpdJob* __restrict__ jobs, const int* __restrict__ prefix, 
 
 int launch_gram_partial_batched(const GramJob* jobs, const int* prefix, int njobs, int items, cudaStream_t st) {
     if (items <= 0) return 0;
-    gram_partial_batched<<<(unsigned)items, 256, 0, st>>>(jobs, prefix, njobs);
+    gram_partial_batched<<<(unsigned)items, 64, 0, st>>>(jobs, prefix, njobs);
     g_launch_count += 1;
     return (int)cudaGetLastError();
 }
