@@ -416,7 +416,11 @@ def run_ours(args, rank, world, local_rank):
         try:
             hx, hr = orth.HostBuffer(m * n * 8), orth.HostBuffer(n * n * 8)
             Xh, Rh = hx.array((m, n)), hr.array((n, n))
-            buf_kind = "page-locked huge-page buffers from orth_gb300_host_alloc"
+            kind, huge = hx.info()
+            buf_kind = ("page-locked huge-page buffers from orth_gb300_host_alloc" if kind == 1 else
+                        "cudaHostAlloc buffers from orth_gb300_host_alloc (huge pages unavailable)")
+            host_buf = {"kind": "huge-page mapping" if kind == 1 else "cudaHostAlloc",
+                        "x_bytes_on_huge_pages": huge, "x_bytes": m * n * 8}
         except RuntimeError:
             # Several ranks on one host may not get that much page-locked memory:
             # the CUDA allocator's page-locked buffers instead.
@@ -424,6 +428,7 @@ def run_ours(args, rank, world, local_rank):
             Xh = torch.empty((n, m), dtype=torch.float64, pin_memory=True).numpy().T
             Rh = torch.zeros((n, n), dtype=torch.float64, pin_memory=True).numpy().T
             buf_kind = "cudaHostAlloc buffers (orth_gb300_host_alloc failed)"
+            host_buf = {"kind": "torch pin_memory"}
         times, timeline = host_leg(Xh, Rh, args.e2e_steps)
         del Xh, Rh
         if hx is not None:
@@ -433,7 +438,7 @@ def run_ours(args, rank, world, local_rank):
         e2e = {"value": round(e2e_ms, 3), "unit": "ms", "samples_ms": [round(x, 1) for x in times],
                "timeline_ms": timeline,
                "h2d_bytes_per_step": m * n * 8, "d2h_bytes_per_step": m * n * 8 + n * n * 8,
-               "path": f"orth.h {variant} (host pointers: {buf_kind}), {prec_name}"}
+               "path": f"orth.h {variant} (host pointers: {buf_kind}), {prec_name}", "host_buffer": host_buf}
         if args.e2e_cuda_host_alloc:
             Xc = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
             Rc = torch.zeros((n, n), dtype=torch.float64, pin_memory=True)

@@ -90,14 +90,23 @@ int orth_gb300_set_host_precision(int precision);
  * pages where the kernel offers them (an aligned anonymous mapping advised
  * MADV_HUGEPAGE, faulted in, then registered with cudaHostRegister): 32 GiB
  * moved at 210 GB/s to a GB300 and 193 GB/s back, against 81-139 GB/s for
- * cudaHostAlloc memory. The memory reads as zero. Returns 0; 2 for a null ptr or
- * zero bytes; 6 if the mapping fails; 3 if the registration fails.
+ * cudaHostAlloc memory. A host too fragmented to give huge pages backs such a
+ * mapping with base pages (25-34 GB/s); when less than 3/4 of a buffer of 64 MB or
+ * more came as huge pages, it is made by cudaHostAlloc instead. The memory reads
+ * as zero. Returns 0; 2 for a null ptr or zero bytes; 6 if the mapping fails; 3 if
+ * the registration or cudaHostAlloc fails.
  * orth_gb300_host_free releases a buffer from orth_gb300_host_alloc (0; 2 for a
  * pointer it did not return; 3 if the unregistration fails; a null pointer is a
  * no-op).
+ * orth_gb300_host_buffer_info reports how a buffer from orth_gb300_host_alloc was
+ * made: *kind = 1 (huge-page mapping, registered) or 2 (cudaHostAlloc), and
+ * *huge_bytes = the bytes of it the kernel backs with huge pages now (-1 if
+ * /proc/self/smaps cannot be read). Returns 0, or 2 for null arguments or a
+ * pointer orth_gb300_host_alloc did not return.
  */
 int orth_gb300_host_alloc(size_t bytes, void **ptr);
 int orth_gb300_host_free(void *ptr);
+int orth_gb300_host_buffer_info(const void *ptr, int *kind, long long *huge_bytes);
 
 /*
  * Row-sharded runs: one rank per GPU, each holding a contiguous block of rows

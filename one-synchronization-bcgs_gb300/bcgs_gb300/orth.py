@@ -106,6 +106,9 @@ def load(path: str | None = None):
     lib.orth_gb300_host_alloc.restype = ctypes.c_int
     lib.orth_gb300_host_free.argtypes = [ctypes.c_void_p]
     lib.orth_gb300_host_free.restype = ctypes.c_int
+    lib.orth_gb300_host_buffer_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                                ctypes.POINTER(ctypes.c_longlong)]
+    lib.orth_gb300_host_buffer_info.restype = ctypes.c_int
     lib.orth_gb300_last_split_error.argtypes = []
     lib.orth_gb300_last_split_error.restype = ctypes.c_int
     lib.orth_gb300_split_supported.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -246,6 +249,15 @@ class HostBuffer:
             raise ValueError("shape exceeds the buffer")
         flat = np.ctypeslib.as_array((ctypes.c_double * count).from_address(self.ptr))
         return flat.reshape(shape, order=order)
+
+    def info(self):
+        """(kind, huge_bytes): 1 for a huge-page mapping or 2 for cudaHostAlloc memory
+        (huge pages unavailable), and the bytes now backed by huge pages (-1 unknown)."""
+        kind, huge = ctypes.c_int(0), ctypes.c_longlong(0)
+        rc = int(load().orth_gb300_host_buffer_info(self._p, ctypes.byref(kind), ctypes.byref(huge)))
+        if rc != 0:
+            raise RuntimeError(f"orth_gb300_host_buffer_info returned {rc}")
+        return int(kind.value), int(huge.value)
 
     def close(self) -> None:
         if self._p.value:

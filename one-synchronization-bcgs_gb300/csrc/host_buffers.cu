@@ -15,13 +15,19 @@
 // orth_gb300_host_alloc makes such a buffer: an anonymous mapping aligned to the
 // huge-page size, advised MADV_HUGEPAGE, faulted in by a few host threads (one
 // write per huge page; the kernel zero-fills), then registered with the CUDA
-// driver (page-locked, usable by async copies). Where huge pages are off the
-// buffer is still pinned, at the base page size. orth_gb300_host_free undoes it.
+// driver (page-locked, usable by async copies). A host whose memory is too
+// fragmented to give huge pages backs such a mapping with base pages, the slow
+// case above; when less than 3/4 of a buffer of 64 MB or more came as huge pages
+// (AnonHugePages in /proc/self/smaps), the mapping is dropped and the buffer comes
+// from cudaHostAlloc instead, zero-filled by the same threads.
+// orth_gb300_host_free undoes either.
 #include <sys/mman.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -35,8 +41,9 @@ namespace bcgs {
 namespace {
 
 struct Mapping {
-    void* raw;
+    void* raw;          // the anonymous mapping (null: a cudaHostAlloc buffer)
     size_t raw_bytes;
+    size_t len;         // usable bytes from the returned pointer
 };
 std::mutex g_host_mu;
 std::map<void*, Mapping> g_host_maps;
@@ -66,7 +73,44 @@ void fault_in(char* p, size_t bytes, size_t step) {
     for (auto& x : th) x.join();
 }
 
+// Zeroes [p, p + bytes) with the same threads.
+void zero_fill(char* p, size_t bytes) {
+    unsigned hw = std::thread::hardware_concurrency();
+    const size_t nt = std::max<size_t>(1, std::min<size_t>(std::min(hw, 16u), (bytes >> 26) + 1));
+    auto work = [&](size_t t) {
+        const size_t b0 = bytes * t / nt, b1 = bytes * (t + 1) / nt;
+        std::memset(p + b0, 0, b1 - b0);
+    };
+    std::vector<std::thread> th;
+    for (size_t t = 1; t < nt; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto& x : th) x.join();
+}
+
 }  // namespace
+
+// Bytes of [p, p + len) backed by transparent huge pages: the AnonHugePages of the
+// mappings that overlap the range (/proc/self/smaps), or -1 if it cannot be read.
+long long huge_backed_bytes(const void* p, size_t len) {
+    FILE* f = std::fopen("/proc/self/smaps", "r");
+    if (!f) return -1;
+    const unsigned long long lo = (unsigned long long)(uintptr_t)p, hi = lo + len;
+    char line[512];
+    bool in = false;
+    long long total = 0;
+    while (std::fgets(line, sizeof line, f)) {
+        unsigned long long a = 0, b = 0;
+        if (std::sscanf(line, "%llx-%llx ", &a, &b) == 2) {   // a mapping's header line
+            in = a < hi && b > lo;
+            continue;
+        }
+        unsigned long long kb = 0;
+        if (in && std::sscanf(line, "AnonHugePages: %llu kB", &kb) == 1) total += (long long)kb * 1024;
+    }
+    std::fclose(f);
+    return total;
+}
+
 }  // namespace bcgs
 
 using namespace bcgs;
@@ -82,6 +126,20 @@ extern "C" int orth_gb300_host_alloc(size_t bytes, void** ptr) {
     char* p = reinterpret_cast<char*>(((uintptr_t)raw + hp - 1) / hp * hp);
     (void)madvise(p, len, MADV_HUGEPAGE);   // best effort: without it the pages are base-size
     fault_in(p, len, hp);
+    const long long huge = huge_backed_bytes(p, len);
+    if (huge >= 0 && bytes >= ((size_t)64 << 20) && (double)huge < 0.75 * (double)len) {
+        munmap(raw, raw_bytes);
+        void* q = nullptr;
+        if (cudaHostAlloc(&q, bytes, cudaHostAllocDefault) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return 3;
+        }
+        zero_fill(static_cast<char*>(q), bytes);
+        std::lock_guard<std::mutex> lock(g_host_mu);
+        g_host_maps[q] = Mapping{nullptr, 0, bytes};
+        *ptr = q;
+        return 0;
+    }
     if (cudaHostRegister(p, len, cudaHostRegisterDefault) != cudaSuccess) {
         (void)cudaGetLastError();
         munmap(raw, raw_bytes);
@@ -89,9 +147,23 @@ extern "C" int orth_gb300_host_alloc(size_t bytes, void** ptr) {
     }
     {
         std::lock_guard<std::mutex> lock(g_host_mu);
-        g_host_maps[p] = Mapping{raw, raw_bytes};
+        g_host_maps[p] = Mapping{raw, raw_bytes, len};
     }
     *ptr = p;
+    return 0;
+}
+
+extern "C" int orth_gb300_host_buffer_info(const void* ptr, int* kind, long long* huge_bytes) {
+    if (ptr == nullptr || kind == nullptr || huge_bytes == nullptr) return 2;
+    Mapping mp;
+    {
+        std::lock_guard<std::mutex> lock(g_host_mu);
+        auto it = g_host_maps.find(const_cast<void*>(ptr));
+        if (it == g_host_maps.end()) return 2;
+        mp = it->second;
+    }
+    *kind = mp.raw ? 1 : 2;
+    *huge_bytes = huge_backed_bytes(ptr, mp.len);
     return 0;
 }
 
@@ -105,6 +177,7 @@ extern "C" int orth_gb300_host_free(void* ptr) {
         mp = it->second;
         g_host_maps.erase(it);
     }
+    if (!mp.raw) return cudaFreeHost(ptr) == cudaSuccess ? 0 : 3;
     const cudaError_t ce = cudaHostUnregister(ptr);
     munmap(mp.raw, mp.raw_bytes);
     return ce == cudaSuccess ? 0 : 3;

@@ -100,6 +100,9 @@ def test_host_buffer_argument_checks(lib):
     assert lib.orth_gb300_host_alloc(ctypes.c_size_t(64), None) == 2
     assert lib.orth_gb300_host_free(None) == 0
     assert lib.orth_gb300_host_free(ctypes.c_void_p(0x12345000)) == 2   # not from orth_gb300_host_alloc
+    kind, huge = ctypes.c_int(0), ctypes.c_longlong(0)
+    assert lib.orth_gb300_host_buffer_info(None, ctypes.byref(kind), ctypes.byref(huge)) == 2
+    assert lib.orth_gb300_host_buffer_info(ctypes.c_void_p(0x12345000), ctypes.byref(kind), ctypes.byref(huge)) == 2
 
 
 def test_split_slice_argument_checks(lib):

@@ -5,6 +5,8 @@ orth_gb300_host_alloc are page-locked and backed by huge pages, so the copies
 run at the host link's full rate. Checked through the C ABI:
   * a fresh buffer reads as zero, is page-locked (the CUDA driver reports it as
     host memory it knows), and is released once (a second free returns 2);
+  * a large buffer is on huge pages, or comes from cudaHostAlloc where the host
+    cannot give them;
   * an orth.h call on such buffers gives Q and R bit-identical to the same call
     on ordinary (pageable) numpy buffers, in FP64 and in the 56-bit split form:
     only the copies differ, not the device computation.
@@ -38,9 +40,29 @@ def test_host_buffer_is_zeroed_pinned_and_freed_once(lib):
     d.copy_(torch.from_numpy(a))
     back = d.cpu().numpy()
     assert np.array_equal(back, a)
+    kind, huge = hb.info()
+    assert kind in (1, 2) and (huge >= 0 or huge == -1)
     p = hb.ptr
     hb.close()
     assert lib.orth_gb300_host_free(ctypes.c_void_p(p)) == 2
+
+
+def test_large_host_buffer_is_huge_page_backed_or_cuda_host_alloc(lib):
+    """A buffer of 1 GiB is either a mapping mostly on huge pages or, where the host
+    cannot give them, cudaHostAlloc memory; it reads as zero either way."""
+    torch = pytest.importorskip("torch")
+    torch.cuda.init()
+    hb = orth.HostBuffer(1 << 30)
+    try:
+        kind, huge = hb.info()
+        if kind == 1 and huge >= 0:
+            assert huge >= 3 * (1 << 30) // 4
+        else:
+            assert kind == 2 or huge == -1
+        a = hb.array((1 << 27,))
+        assert not a[:: 4096].any() and not a[-1]
+    finally:
+        hb.close()
 
 
 @pytest.mark.parametrize("precision", ["fp64", "split7"])
