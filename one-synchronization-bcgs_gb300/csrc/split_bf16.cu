@@ -82,21 +82,19 @@ constexpr int UTHREADS = 64 + UNEPI;        // update: producer + MMA warps + ep
 // ---------------------------------------------------------------------------
 template <int KD>
 __device__ __forceinline__ long long fixed_point_of(double x, int e) {
-    // V = round(x * 2^{8 KD - 1 - e}) from the FP64 bit pattern (|x| < 2^e).
+    // V = round(x * 2^{8 KD - 1 - e}) from the FP64 bit pattern, half away from
+    // zero. With |x| < 2^e the mantissa's shift sh = E - 1075 + 8 KD - 1 - e is at
+    // most 2, so k = 3 - sh >= 1 and V = (8 M + 2^{k-1}) >> k (exact for sh >= 0,
+    // rounded for sh < 0). k is clamped to 63, where the quotient is already 0
+    // (8 M < 2^56). Zero, subnormals, Inf and NaN give 0.
     const long long bits = __double_as_longlong(x);
     const int E = (int)((bits >> 52) & 0x7FF);
-    long long V = 0;
-    if (E != 0 && E != 0x7FF) {
-        const unsigned long long M = (unsigned long long)(bits & 0xFFFFFFFFFFFFFLL) | (1ULL << 52);
-        int sh = E - 1075 + 8 * KD - 1 - e;  // V = M * 2^sh
-        if (sh > 9) sh = 9;
-        if (sh >= 0)
-            V = (long long)(M << sh);
-        else if (sh > -60)
-            V = (long long)((M + (1ULL << (-sh - 1))) >> (-sh));
-        if (bits < 0) V = -V;
-    }
-    return V;
+    if (E == 0 || E == 0x7FF) return 0;
+    const unsigned long long M8 = ((unsigned long long)(bits & 0xFFFFFFFFFFFFFLL) | (1ULL << 52)) << 3;
+    int k = 3 - (E - 1075 + 8 * KD - 1 - e);
+    k = k < 1 ? 1 : (k > 63 ? 63 : k);
+    const long long V = (long long)((M8 + (1ULL << (k - 1))) >> k);
+    return bits < 0 ? -V : V;
 }
 
 // Balanced digits d_0 (most significant) .. d_{KD-1} in [-128, 128] of V. With the
